@@ -1,0 +1,314 @@
+"""Benchmark of the render-and-encode hot path (one JSON line on rank 0).
+
+Workload (the plain GPU drop-in configuration): the seeded scene (seed 0,
+16 levels x 2^19 entries), one 1920x1080 mono view per request, 100 poses
+uniform on the radius-1.5 sphere looking at the cube centre, 90 deg
+horizontal FOV.  A step is one request: ray generation + march + composite
+into RGB/depth, RGB24 quantisation, RGB24->YUV420P and depth packing to
+uint16 mm, all on the device with the scene resident.  L2 is flushed (a
+256 MiB write) before every timed step, outside the timed interval.
+
+  value   Mrays/s (all pixels, misses included) of the device step, from
+          CUDA events on the launching stream, summed over K steps, max over
+          ranks, times the number of ranks (weak scaling: each rank renders
+          its own requests).
+  e2e     the same metric through nes_render_yuv (pose in host memory, YUV
+          planes + packed depth copied back to pinned host buffers inside
+          the timed region), plus p50/p99 pose->YUV latency.
+
+--impl reference times the CPU restatement of the path (oracle/, FP64,
+all host threads) on bounded random pixel samples of the same requests: the
+reference's renderer is an external project and its swscale/libavcodec
+dependencies are not installed, so the oracle port is the CPU arm.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "ngp-encode-server_gb300"))
+
+W, H, FOV, NPOSES, RADIUS = 1920, 1080, 90.0, 100, 1.5
+FLOP_PER_SAMPLE = 18688          # 2 x 9,344 MLP multiply-adds
+GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
+WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", choices=["auto", "fp32", "tc"], default="auto")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=None)
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.lines, self.proc = device, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) != 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return pk["hbm_gbs"], pk["bf16_tflops"], pk["bf16_tflops_sustained"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def cpu_sample(poses, steps_px, seed):
+    """Times the FP64 oracle on random pixel subsets; returns (Mrays/s, s, px, threads)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import numpy as np
+    import nes
+    import oracle
+    scene = oracle.Scene(0, 19)
+    f = nes.focal_from_fov(W, FOV)
+    rng = np.random.default_rng(seed)
+    threads = os.cpu_count() or 1
+    total_px, total_s = 0, 0.0
+    for i, npx in enumerate(steps_px):
+        pix = rng.choice(W * H, npx, replace=False).astype(np.int32)
+        t0 = time.perf_counter()
+        scene.render(poses[i % len(poses)], W, H, f, pixels=pix, nthreads=threads)
+        total_s += time.perf_counter() - t0
+        total_px += npx
+    return total_px / total_s / 1e6, total_s, total_px, threads
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import nes
+    poses = nes.shell_poses(0, NPOSES, RADIUS, RADIUS)
+    per_step = max(2048, (W * H) // 256)
+    cpu_sample(poses, [per_step // 4] * max(1, args.warmup), 99)  # warm-up
+    mrays, secs, px, threads = cpu_sample(poses, [per_step] * args.steps, 1)
+    line = {"metric": "Mrays/s (pose->YUV render, all pixels)", "value": round(mrays, 6), "unit": "Mrays/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene and poses)",
+            "config": {"workload": WORKLOAD, "sample": "%d random pixels per step" % per_step,
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": round(mrays, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": "%d random pixels of a 1920x1080 request per step, %d steps" % (per_step,
+                                                                                                   args.steps)},
+            "e2e": {"value": round(mrays, 6), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import nes
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(dev)  # a real stream: NULL would mean the library's own
+    torch.cuda.set_stream(stream)
+    precisions = {"fp32": [nes.PREC_FP32], "tc": [nes.PREC_FP16_TC],
+                  "auto": [nes.PREC_FP16_TC, nes.PREC_FP32]}[args.precision]
+
+    poses = nes.shell_poses(rank, NPOSES, RADIUS, RADIUS)  # each rank serves its own requests
+    focal = nes.focal_from_fov(W, FOV)
+    views = [nes.make_view(m, W, H, focal) for m in poses]
+    ls = nes.linesizes(W)
+    ch = (H + 1) // 2
+    rgb = torch.empty(W * H * 3, device=dev)
+    dep = torch.empty(W * H, device=dev)
+    rgb8 = torch.empty(W * H * 3, dtype=torch.uint8, device=dev)
+    yuv = torch.empty(ls[0] * H + (ls[1] + ls[2]) * ch, dtype=torch.uint8, device=dev)
+    dmm = torch.empty(W * H, dtype=torch.int16, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    lib = nes.load()
+    yp, up, vp = yuv.data_ptr(), yuv.data_ptr() + ls[0] * H, yuv.data_ptr() + ls[0] * H + ls[1] * ch
+    sptr = stream.cuda_stream
+
+    results, renderer_used = {}, None
+    for prec in precisions:
+        try:
+            r = nes.Renderer(precision=prec, max_pixels=W * H, device=local)
+        except nes.NesError as e:
+            results[prec] = {"error": str(e)}
+            continue
+        r.set_profiling(True)
+
+        def step(i):
+            r.render_views([views[i % NPOSES]], [rgb.data_ptr()], [dep.data_ptr()], sptr)
+            nes.check(lib.nes_rgb_to_rgb24(rgb.data_ptr(), W * H * 3, rgb8.data_ptr(), sptr), "rgb24")
+            nes.rgb24_to_yuv420p(rgb8.data_ptr(), W, H, W * 3, yp, up, vp, ls, sptr)
+            nes.depth_pack_u16mm(dep.data_ptr(), W * H, dmm.data_ptr(), sptr)
+
+        try:
+            for i in range(args.warmup):
+                flush.zero_()
+                step(i)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            march_ms, raygen_ms, samples = [], [], []
+            with ClockSampler(local) as clk:
+                for i in range(args.steps):
+                    flush.zero_()
+                    ev[i][0].record(stream)
+                    step(i)
+                    ev[i][1].record(stream)
+                    rg, mm = r.last_timings()
+                    raygen_ms.append(rg)
+                    march_ms.append(mm)
+                    samples.append(r.last_sample_count())
+                torch.cuda.synchronize()
+            step_ms = [a.elapsed_time(b) for a, b in ev]
+            total_ms = sum(step_ms)
+            if world > 1:
+                t = torch.tensor([total_ms], device=dev)
+                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+                total_ms = float(t.item())
+            res = {"total_ms": total_ms, "ms_per_step": total_ms / args.steps,
+                   "mrays": world * W * H * args.steps / (total_ms / 1e3) / 1e6,
+                   "march_ms": statistics.mean(march_ms), "raygen_ms": statistics.mean(raygen_ms),
+                   "samples_per_step": statistics.mean(samples), "clocks": clk.summary()}
+
+            # End to end through the host-buffer C-ABI call.
+            ke = args.e2e_steps or args.steps
+            hy = torch.empty(ls[0] * H, dtype=torch.uint8).pin_memory()
+            hu = torch.empty(ls[1] * ch, dtype=torch.uint8).pin_memory()
+            hv = torch.empty(ls[2] * ch, dtype=torch.uint8).pin_memory()
+            hd = torch.empty(W * H, dtype=torch.int16).pin_memory()
+            r.set_profiling(False)
+            for i in range(args.warmup):
+                r.render_yuv(views[i % NPOSES], hy.data_ptr(), hu.data_ptr(), hv.data_ptr(), ls, hd.data_ptr())
+            lat = []
+            for i in range(ke):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                r.render_yuv(views[i % NPOSES], hy.data_ptr(), hu.data_ptr(), hv.data_ptr(), ls, hd.data_ptr())
+                lat.append(time.perf_counter() - t0)
+            lat_sorted = sorted(lat)
+            res["e2e"] = {"mrays": world * W * H * ke / sum(lat) / 1e6,
+                          "p50_ms": 1e3 * lat_sorted[len(lat) // 2],
+                          "p99_ms": 1e3 * lat_sorted[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)],
+                          "h2d": 48 + 8, "d2h": hy.numel() + hu.numel() + hv.numel() + 2 * hd.numel()}
+            results[prec] = res
+            if renderer_used is None:
+                renderer_used = prec
+        finally:
+            r.close()
+
+    if rank != 0:
+        return
+    if renderer_used is None:
+        print(json.dumps({"metric": "Mrays/s (pose->YUV render, all pixels)", "value": None,
+                          "error": {str(k): v for k, v in results.items()}}), flush=True)
+        sys.exit(1)
+    head = results[renderer_used]
+    hbm, tf_burst, tf_sust, src = load_peaks()
+    kind = "fp16" if renderer_used == nes.PREC_FP16_TC else "fp32"
+    achieved = head["samples_per_step"] * FLOP_PER_SAMPLE / (head["march_ms"] / 1e3) / 1e12
+    line = {
+        "metric": "Mrays/s (pose->YUV render, all pixels)", "value": round(head["mrays"], 3), "unit": "Mrays/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(head["ms_per_step"], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": kind, "data": "synthetic (seeded scene and poses)",
+        "config": {"workload": WORKLOAD, "precision": "FP16 tcgen05" if kind == "fp16" else "FP32 CUDA cores",
+                   "l2": "flushed (256 MiB write) before every timed step", "parallelism": "replicas"},
+        "e2e": {"value": round(head["e2e"]["mrays"], 3), "unit": "Mrays/s",
+                "h2d_bytes_per_step": head["e2e"]["h2d"], "d2h_bytes_per_step": head["e2e"]["d2h"],
+                "p50_ms": round(head["e2e"]["p50_ms"], 3), "p99_ms": round(head["e2e"]["p99_ms"], 3)},
+        "gpu_launches": 5 * args.steps,
+        "roofline": {"bound": "tensor", "achieved": round(achieved, 3), "peak": tf_sust, "unit": "TFLOP/s",
+                     "frac": round(achieved / tf_sust, 5), "traffic": None,
+                     "kernel": "march", "peak_source": src + " bf16 sustained",
+                     "march_ms": round(head["march_ms"], 3), "raygen_ms": round(head["raygen_ms"], 4),
+                     "samples_per_step": int(head["samples_per_step"]),
+                     "gather_gbs": round(head["samples_per_step"] * GATHER_BYTES[kind] / (head["march_ms"] / 1e3) / 1e9, 1)},
+        "clocks": head["clocks"],
+        "paths": {("fp16_tc" if k == nes.PREC_FP16_TC else "fp32"):
+                  ({"mrays": round(v["mrays"], 3), "ms_per_step": round(v["ms_per_step"], 3),
+                    "e2e_mrays": round(v["e2e"]["mrays"], 3), "p99_ms": round(v["e2e"]["p99_ms"], 3)}
+                   if "mrays" in v else v) for k, v in results.items()},
+    }
+    if not args.no_cpu_baseline:
+        per = (W * H) // 32
+        mrays, secs, px, threads = cpu_sample(poses, [per], 7)
+        line["cpu_baseline"] = {"value": round(mrays, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                "sample": "%d random pixels of one 1920x1080 request (FP64 oracle, %.1f s)" % (px, secs)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,213 @@
+/*
+ * nes_gb300.h -- C ABI of the GB300 render-and-encode library.
+ *
+ * Two drop-in boundaries of neserver (moonsikpark/ngp-encode-server):
+ *
+ *  (i)  The renderer round trip.  neserver serialises a nesproto::FrameRequest,
+ *       sends it length-prefixed to an external instant-ngp-renderer process
+ *       and parses the nesproto::RenderedFrame it gets back
+ *       (src/server.cpp:161-194, framing in src/server.cpp:46-60 and 91-112).
+ *       nes_render() takes and returns the same nes.proto bytes
+ *       (proto/nes.proto:5-25) in-process; nes_render_views() and
+ *       nes_render_yuv() are the device-native forms.
+ *
+ *  (ii) The frame glue.  RenderedFrame::convert_frame converts the RGB24 scene
+ *       and GRAY8 depth planes to YUV420P with libswscale
+ *       (include/base/video/rendered_frame.h:24-33,
+ *       src/base/video/type_managers.cc:241-251).  nes_rgb24_to_yuv420p() and
+ *       nes_gray8_to_yuv420p() write the same YUV420P plane layout that
+ *       AVCodecContextManager::send_frame consumes (src/encode.cpp:136-137,
+ *       164-165); nes_depth_pack_u16mm() packs FP32 depth to uint16 mm.
+ *
+ * Conventions (mirroring src/server.cpp:23-43, which returns -errno):
+ *  - every entry point returns an int status: NES_OK (0) or a negative
+ *    errno-style NES_E* code; no C++ exception crosses this boundary;
+ *  - pointers named *_dev are CUDA device pointers, everything else is host;
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the context's own
+ *    stream (stream-free glue functions use the legacy default stream);
+ *  - one nes_ctx may be used from several host threads; calls on one context
+ *    are serialised internally.
+ */
+#ifndef NES_GB300_H_
+#define NES_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NES_OK 0
+#define NES_EIO (-5)        /* a CUDA call failed */
+#define NES_EAGAIN (-11)    /* nothing ready yet / queue full */
+#define NES_ENOMEM (-12)    /* device or host allocation failed */
+#define NES_ENODEV (-19)    /* no usable CUDA device */
+#define NES_EINVAL (-22)    /* bad argument */
+#define NES_EPROTO (-71)    /* malformed nes.proto message */
+#define NES_ENOBUFS (-105)  /* caller's output buffer too small */
+#define NES_ETIMEDOUT (-110)/* a bounded wait ran out */
+
+enum nes_precision {
+  NES_PREC_FP32 = 0,    /* plain path: FP32 table, FP32 MLP on CUDA cores */
+  NES_PREC_FP16_TC = 1  /* FP16 table, FP16 MLP on tcgen05 tensor cores, FP32 accumulate */
+};
+
+typedef struct nes_ctx nes_ctx;
+
+/* Scene and renderer configuration.  The scene is generated from `seed`
+ * (SplitMix64 streams) and is identical for every precision. */
+typedef struct nes_config {
+  uint64_t seed;             /* scene seed (0 for the reference scene) */
+  uint32_t log2_table_size;  /* hash-table entries per level = 2^this (10..24) */
+  int32_t precision;         /* enum nes_precision */
+  float fov_deg;             /* horizontal FOV for nes_render (nes.proto has no FOV field) */
+  float depth_gray_max;      /* scene units mapped to 255 in GRAY8 depth */
+  int32_t device;            /* CUDA device ordinal */
+  uint32_t max_pixels;       /* largest single-call pixel count (sum over views) */
+} nes_config;
+
+/* One view to render: the nes.proto Camera plus a focal length.
+ * matrix: 3x4 row-major pose (include/base/camera_manager.h:18-19):
+ * columns 0,1,2 = image right, image down, view direction; column 3 = eye. */
+typedef struct nes_view {
+  float matrix[12];
+  uint32_t width;
+  uint32_t height;
+  float focal_px;  /* focal length in pixels; see nes_focal_from_fov */
+  uint32_t flags;  /* reserved, 0 */
+} nes_view;
+
+/* Fills cfg with the reference scene: seed 0, 2^19 entries, FP32, 90 deg. */
+void nes_config_default(nes_config *cfg);
+
+/* Creates a context on cfg->device: generates the scene, uploads it,
+ * builds the 128^3 occupancy grid.  Replaces connecting to a renderer
+ * (src/server.cpp:216-283). */
+int nes_create(const nes_config *cfg, nes_ctx **out);
+void nes_destroy(nes_ctx *ctx);
+const char *nes_strerror(int code);
+
+/* focal = (width/2) / tan(fov/2), computed in double, rounded to float. */
+float nes_focal_from_fov(uint32_t width, float fov_deg);
+
+/* ---------------- (i) renderer round trip ---------------- */
+
+/* Upper bound of the RenderedFrame bytes nes_render writes for a w x h
+ * camera (RGB24 frame + GRAY8 depth + header). */
+size_t nes_rendered_frame_capacity(uint32_t width, uint32_t height);
+
+/* Wire-compatible render: request = serialised nesproto::FrameRequest,
+ * frame_out receives a serialised nesproto::RenderedFrame with the same
+ * index/camera/is_left, frame = RGB24 (W*H*3) and depth = GRAY8 (W*H),
+ * exactly the payload src/server.cpp:193-194 wraps.  Replaces
+ * socket_send_blocking_lpf + socket_receive_blocking_lpf + ParseFromString
+ * (src/server.cpp:161-177).  NES_EPROTO for a malformed request,
+ * NES_ENOBUFS (with *frame_len = bytes needed) when cap is too small. */
+int nes_render(nes_ctx *ctx, const uint8_t *request, size_t request_len, uint8_t *frame_out,
+               size_t frame_cap, size_t *frame_len);
+
+/* Device-native render of n views in one batch (rays of all views share
+ * one march).  rgb_dev[i]: W*H*3 floats (HWC), depth_dev[i]: W*H floats
+ * (expected depth, 0 for rays that miss); either may be NULL. */
+int nes_render_views(nes_ctx *ctx, const nes_view *views, int nviews, float *const *rgb_dev,
+                     float *const *depth_dev, void *stream);
+
+/* Pose -> YUV end to end for one view: render, RGB24 quantise, convert to
+ * YUV420P and pack depth to uint16 mm on the device, then copy the planes to
+ * the caller's HOST buffers (pinned for best speed).  y/u/v follow
+ * linesize[3] (chroma planes are ceil(W/2) x ceil(H/2)); depth_mm_host is
+ * W*H uint16 (may be NULL).  Blocks until the host buffers are filled. */
+int nes_render_yuv(nes_ctx *ctx, const nes_view *view, uint8_t *y_host, uint8_t *u_host,
+                   uint8_t *v_host, const int linesize[3], uint16_t *depth_mm_host);
+
+/* ---------------- (ii) frame glue ---------------- */
+
+/* RGB24 -> YUV420P, BT.601 studio range, 2x2 chroma average (edge pixels
+ * replicated for odd sizes).  Replaces the scene SwsContextManager in
+ * RenderedFrame::convert_frame (include/base/video/rendered_frame.h:28-29). */
+int nes_rgb24_to_yuv420p(const uint8_t *rgb_dev, int width, int height, int rgb_linesize,
+                         uint8_t *y_dev, uint8_t *u_dev, uint8_t *v_dev, const int linesize[3],
+                         void *stream);
+
+/* GRAY8 -> YUV420P (luma scaled to studio range, chroma 128).  Replaces the
+ * depth SwsContextManager (include/base/video/rendered_frame.h:30-31). */
+int nes_gray8_to_yuv420p(const uint8_t *gray_dev, int width, int height, int gray_linesize,
+                         uint8_t *y_dev, uint8_t *u_dev, uint8_t *v_dev, const int linesize[3],
+                         void *stream);
+
+/* FP32 depth (scene units = metres) -> uint16 millimetres, round half up,
+ * NaN/negative -> 0, saturating at 65535. */
+int nes_depth_pack_u16mm(const float *depth_dev, size_t n, uint16_t *out_dev, void *stream);
+
+/* FP32 depth -> GRAY8 (round(clamp(d/dmax,0,1)*255)), the depth plane of
+ * nesproto::RenderedFrame (src/server.cpp:193-194). */
+int nes_depth_to_gray8(const float *depth_dev, size_t n, float dmax, uint8_t *out_dev,
+                       void *stream);
+
+/* FP32 RGB in [0,1] -> RGB24 bytes (round(clamp(x,0,1)*255)). */
+int nes_rgb_to_rgb24(const float *rgb_dev, size_t n, uint8_t *out_dev, void *stream);
+
+/* ---------------- nes.proto wire helpers (no GPU) ---------------- */
+
+/* A parsed nesproto::FrameRequest (proto/nes.proto:12-16) with its Camera
+ * (proto/nes.proto:5-10) flattened. */
+typedef struct nes_frame_request {
+  uint64_t index;
+  int32_t is_left;
+  int32_t has_camera;
+  int32_t camera_is_left;
+  uint32_t width;
+  uint32_t height;
+  uint32_t matrix_len;  /* floats present in Camera.matrix; 12 expected */
+  float matrix[12];     /* the first min(12, matrix_len) floats */
+} nes_frame_request;
+
+/* Parses FrameRequest bytes, as the renderer side of src/server.cpp:161-168
+ * receives them.  NES_EPROTO on malformed input. */
+int nes_parse_frame_request(const uint8_t *bytes, size_t len, nes_frame_request *out);
+
+/* Serialises RenderedFrame{index, camera, is_left, frame, depth}
+ * (proto/nes.proto:18-25) echoing req's index/camera/is_left, as the renderer
+ * answers src/server.cpp:170-177.  *out_len = bytes needed; NES_ENOBUFS when
+ * cap is too small (out may then be NULL). */
+int nes_write_rendered_frame(const nes_frame_request *req, const uint8_t *frame, size_t frame_len,
+                             const uint8_t *depth, size_t depth_len, uint8_t *out, size_t cap,
+                             size_t *out_len);
+
+/* Generates the seeded scene on the host (no GPU): table = 16*2^log2T*2
+ * floats (level-major), weights = 9408 floats: density W1 [64][32], density
+ * W2 [16][64], colour W1 [64][32], colour W2 [64][64], colour W3 [3][64]. */
+int nes_scene_generate(uint64_t seed, uint32_t log2_table_size, float *table_out, float *weights_out);
+
+/* ---------------- scene access (tests, tools) ---------------- */
+
+/* Copies one scene parameter array to host: which 0 = hash table
+ * (16*T*2 floats, level-major), 1..5 = density W1 [64][32], density W2
+ * [16][64], colour W1 [64][32] (column 31 zero), colour W2 [64][64],
+ * colour W3 [3][64] (row-major [out][in]). */
+int nes_scene_param(nes_ctx *ctx, int which, float *host_out, size_t count);
+
+/* Copies the 128^3 occupancy bitfield (65536 uint32 words, x-fastest). */
+int nes_occupancy(nes_ctx *ctx, uint32_t *host_bits);
+
+/* Rebuilds the occupancy grid with a different density threshold
+ * (the scene's own threshold is 0.01). */
+int nes_rebuild_occupancy(nes_ctx *ctx, float threshold);
+
+/* Number of field evaluations (samples) of the last render call. */
+int nes_last_sample_count(nes_ctx *ctx, uint64_t *samples);
+
+/* Per-kernel timing with CUDA events recorded on the stream the kernels
+ * run on (the reference's ScopedTimer averages, src/server.cpp:172-190,
+ * in device time).  When enabled, every render records events around ray
+ * generation and the march; nes_last_timings waits for the last render and
+ * returns both durations in milliseconds. */
+int nes_set_profiling(nes_ctx *ctx, int enable);
+int nes_last_timings(nes_ctx *ctx, float *raygen_ms, float *march_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NES_GB300_H_ */

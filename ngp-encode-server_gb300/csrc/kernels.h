@@ -1,0 +1,69 @@
+// kernels.h -- host-side launchers of the CUDA kernels (one declaration per
+// kernel family).  All launchers are asynchronous on `stream` and return the
+// launch's cudaError_t.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "render_common.cuh"
+
+namespace nes {
+
+// Device-resident scene handles used by every render kernel.
+struct DevScene {
+  const float2* table32 = nullptr;  // [16][T] float2
+  const __half2* table16 = nullptr; // [16][T] half2 (tensor-core path)
+  const float* weights = nullptr;   // kWeightFloats FP32 blob
+  const uint8_t* tc_weights = nullptr; // FP16 weights in the MMA operand layout
+  const uint32_t* occ = nullptr;    // kOccWords
+  uint32_t T = 0;
+  uint32_t dense_mask = 0;
+};
+
+// Per-call scratch shared by the render kernels.
+struct DevScratch {
+  float4* ray_dt = nullptr;   // compacted rays: direction + t_start
+  RayMeta* ray_meta = nullptr;
+  uint32_t* counters = nullptr;  // [0] rays, [1] work cursor, [2..3] samples (u64)
+  uint32_t max_rays = 0;
+};
+
+// Counter slots inside DevScratch::counters.
+constexpr int kCtrRays = 0;
+constexpr int kCtrCursor = 1;
+constexpr int kCtrSamples = 2;  // 64-bit, occupies words 2 and 3
+constexpr int kCtrWords = 8;
+
+// Ray generation + unit-cube clip + warp-ballot compaction of hits; writes
+// zero colour/depth for pixels whose ray misses.  counters must be zeroed.
+cudaError_t launch_raygen(const ViewBatch& views, const DevScratch& s, cudaStream_t stream);
+
+// Plain FP32 march: persistent CTAs pull compacted rays, evaluate the FP32
+// table + FP32 MLP on CUDA cores and composite.
+cudaError_t launch_march_fp32(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
+                              int num_sms, cudaStream_t stream);
+
+// FP16 tensor-core march (tcgen05 MLP).
+cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
+                            int num_sms, cudaStream_t stream);
+
+// 128^3 occupancy bitfield from the FP32 density at cell centres.
+cudaError_t launch_occupancy(const DevScene& scene, float threshold, uint32_t* occ_out,
+                             cudaStream_t stream);
+
+// Frame glue.
+cudaError_t launch_rgb24_to_yuv420p(const uint8_t* rgb, int w, int h, int rgb_ls, uint8_t* y,
+                                    uint8_t* u, uint8_t* v, const int ls[3], cudaStream_t stream);
+cudaError_t launch_gray8_to_yuv420p(const uint8_t* g, int w, int h, int g_ls, uint8_t* y, uint8_t* u,
+                                    uint8_t* v, const int ls[3], cudaStream_t stream);
+cudaError_t launch_depth_pack_u16mm(const float* d, size_t n, uint16_t* out, cudaStream_t stream);
+cudaError_t launch_depth_to_gray8(const float* d, size_t n, float dmax, uint8_t* out,
+                                  cudaStream_t stream);
+cudaError_t launch_rgb_to_rgb24(const float* rgb, size_t n, uint8_t* out, cudaStream_t stream);
+
+// FP32 -> FP16 table conversion (level-major, same indexing).
+cudaError_t launch_table_to_fp16(const float2* src, __half2* dst, size_t n, cudaStream_t stream);
+
+}  // namespace nes

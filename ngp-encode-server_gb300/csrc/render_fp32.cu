@@ -1,0 +1,275 @@
+// render_fp32.cu -- ray generation + compaction, the plain FP32 march
+// (CUDA cores only), the occupancy-grid build and the FP16 table copy.
+//
+// These kernels stand in for the external instant-ngp-renderer that
+// neserver reaches over TCP (src/server.cpp:161-194): a FrameRequest's
+// camera becomes one ray per pixel, rays that miss the unit cube are dropped
+// by a warp-ballot prefix sum, and the survivors are marched through the
+// hash-grid field and composited into RGB and expected depth.
+#include <cuda_fp16.h>
+
+#include "kernels.h"
+
+namespace nes {
+
+namespace {
+
+constexpr int kRaygenThreads = 256;
+constexpr int kMarchThreads = 128;
+
+__global__ void __launch_bounds__(kRaygenThreads)
+raygen_kernel(const ViewBatch vb, float4* __restrict__ ray_dt, RayMeta* __restrict__ ray_meta,
+              uint32_t* __restrict__ counters, uint32_t max_rays) {
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = gid < vb.total_pixels;
+  int v = 0;
+  if (valid)
+    while (v + 1 < vb.n && gid >= vb.v[v + 1].pix_offset) ++v;
+  int n = 0, pix = 0;
+  float3 o, d;
+  float ts = 0.0f;
+  if (valid) {
+    const DevView& V = vb.v[v];
+    pix = (int)(gid - V.pix_offset);
+    const int px = pix % V.W, py = pix / V.W;
+    n = ray_setup(V.M, V.W, V.H, V.focal, px, py, o, d, ts);
+    if (n == 0) {  // miss: nothing to march, the pixel is black at depth 0
+      if (V.rgb) {
+        V.rgb[(size_t)pix * 3 + 0] = 0.0f;
+        V.rgb[(size_t)pix * 3 + 1] = 0.0f;
+        V.rgb[(size_t)pix * 3 + 2] = 0.0f;
+      }
+      if (V.depth) V.depth[pix] = 0.0f;
+    }
+  }
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned mask = __ballot_sync(0xffffffffu, n > 0);
+  if (mask == 0) return;
+  const int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(counters + kCtrRays, (uint32_t)__popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (n > 0) {
+    const uint32_t slot = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+    if (slot < max_rays) {
+      ray_dt[slot] = make_float4(d.x, d.y, d.z, ts);
+      ray_meta[slot] = RayMeta{v, pix, n, 0};
+    }
+  }
+}
+
+// FP32 weights in shared memory, laid out for broadcast float4 reads.
+struct SmemWeights32 {
+  float dw1[kHid * kEnc];    // [j][k]
+  float dw2t[kHid * kDOut];  // [j][m] (transposed)
+  float cw1[kHid * kCIn];    // [j][k]
+  float cw2[kHid * kHid];    // [j][k]
+  float cw3t[kHid * 4];      // [j][c], c = 3 padded
+};
+
+__device__ void load_weights32(SmemWeights32& W, const float* __restrict__ g) {
+  for (int i = threadIdx.x; i < kHid * kEnc; i += blockDim.x) W.dw1[i] = g[kOffDW1 + i];
+  for (int i = threadIdx.x; i < kHid * kDOut; i += blockDim.x) {
+    const int j = i / kDOut, m = i % kDOut;
+    W.dw2t[i] = g[kOffDW2 + m * kHid + j];
+  }
+  for (int i = threadIdx.x; i < kHid * kCIn; i += blockDim.x) W.cw1[i] = g[kOffCW1 + i];
+  for (int i = threadIdx.x; i < kHid * kHid; i += blockDim.x) W.cw2[i] = g[kOffCW2 + i];
+  for (int i = threadIdx.x; i < kHid * 4; i += blockDim.x) {
+    const int j = i / 4, c = i % 4;
+    W.cw3t[i] = c < 3 ? g[kOffCW3 + c * kHid + j] : 0.0f;
+  }
+}
+
+__device__ __forceinline__ float dot32(const float* __restrict__ w, const float in[32]) {
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+  float a = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float4 q = w4[k];
+    a = fmaf(q.x, in[4 * k + 0], a);
+    a = fmaf(q.y, in[4 * k + 1], a);
+    a = fmaf(q.z, in[4 * k + 2], a);
+    a = fmaf(q.w, in[4 * k + 3], a);
+  }
+  return a;
+}
+
+// Density MLP 32->64->16 (ReLU hidden), FP32.
+__device__ __forceinline__ void density_mlp32(const SmemWeights32& W, const float enc[32], float out[16]) {
+#pragma unroll
+  for (int m = 0; m < kDOut; ++m) out[m] = 0.0f;
+#pragma unroll 4
+  for (int j = 0; j < kHid; ++j) {
+    const float a = fmaxf(dot32(W.dw1 + j * kEnc, enc), 0.0f);
+    const float4* w2 = reinterpret_cast<const float4*>(W.dw2t + j * kDOut);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 q = w2[k];
+      out[4 * k + 0] = fmaf(q.x, a, out[4 * k + 0]);
+      out[4 * k + 1] = fmaf(q.y, a, out[4 * k + 1]);
+      out[4 * k + 2] = fmaf(q.z, a, out[4 * k + 2]);
+      out[4 * k + 3] = fmaf(q.w, a, out[4 * k + 3]);
+    }
+  }
+}
+
+// Colour MLP [SH16 | out[1..15] | 0] 32->64->64->3, FP32.
+__device__ __forceinline__ float3 colour_mlp32(const SmemWeights32& W, const float sh[16],
+                                               const float dout[16]) {
+  float cin[32];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) cin[k] = sh[k];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) cin[16 + k] = dout[1 + k];
+  cin[31] = 0.0f;
+  float g1[kHid];
+#pragma unroll
+  for (int j = 0; j < kHid; ++j) g1[j] = fmaxf(dot32(W.cw1 + j * kCIn, cin), 0.0f);
+  float r = 0.0f, g = 0.0f, b = 0.0f;
+#pragma unroll 2
+  for (int j = 0; j < kHid; ++j) {
+    const float4* w4 = reinterpret_cast<const float4*>(W.cw2 + j * kHid);
+    float a = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const float4 q = w4[k];
+      a = fmaf(q.x, g1[4 * k + 0], a);
+      a = fmaf(q.y, g1[4 * k + 1], a);
+      a = fmaf(q.z, g1[4 * k + 2], a);
+      a = fmaf(q.w, g1[4 * k + 3], a);
+    }
+    a = fmaxf(a, 0.0f);
+    const float4 c3 = *reinterpret_cast<const float4*>(W.cw3t + j * 4);
+    r = fmaf(c3.x, a, r);
+    g = fmaf(c3.y, a, g);
+    b = fmaf(c3.z, a, b);
+  }
+  return make_float3(sigmoidf(r), sigmoidf(g), sigmoidf(b));
+}
+
+__global__ void __launch_bounds__(kMarchThreads)
+march_fp32_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
+  extern __shared__ float4 smem_raw[];
+  SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
+  load_weights32(W, sc.weights);
+  __syncthreads();
+
+  const uint32_t nrays = min(s.counters[kCtrRays], s.max_rays);
+  const unsigned lane = threadIdx.x & 31u;
+  unsigned long long my_samples = 0;
+  for (;;) {
+    const uint32_t base = warp_claim(s.counters + kCtrCursor, 32);
+    if (base >= nrays) break;
+    const uint32_t r = base + lane;
+    if (r < nrays) {
+    const float4 rd = s.ray_dt[r];
+    const RayMeta m = s.ray_meta[r];
+    const DevView& V = vb.v[m.view];
+    const float3 o = make_float3(V.M[3], V.M[7], V.M[11]);
+    const float3 d = make_float3(rd.x, rd.y, rd.z);
+    float sh[16];
+    sh16(d, sh);
+    float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f, dep = 0.0f;
+    for (int i = 0; i < m.n; ++i) {
+      const float t = fmaf((float)i + 0.5f, kDt, rd.w);
+      const float3 x = sample_pos(o, d, t);
+      if (!occupied(sc.occ, x)) continue;
+      float enc[kEnc];
+      encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
+      float dout[kDOut];
+      density_mlp32(W, enc, dout);
+      const float sigma = expf(dout[0] - 1.0f);
+      const float3 c = colour_mlp32(W, sh, dout);
+      ++my_samples;
+      const float alpha = -expm1f(-sigma * kDt);
+      const float w = T * alpha;
+      cr = fmaf(w, c.x, cr);
+      cg = fmaf(w, c.y, cg);
+      cb = fmaf(w, c.z, cb);
+      dep = fmaf(w, t, dep);
+      T -= w;
+      if (T < kTStop) break;
+    }
+    if (V.rgb) {
+      V.rgb[(size_t)m.pixel * 3 + 0] = cr;
+      V.rgb[(size_t)m.pixel * 3 + 1] = cg;
+      V.rgb[(size_t)m.pixel * 3 + 2] = cb;
+    }
+    if (V.depth) V.depth[m.pixel] = dep;
+    }
+  }
+  // One 64-bit atomic per warp for the sample count.
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) my_samples += __shfl_down_sync(0xffffffffu, my_samples, off);
+  if (lane == 0 && my_samples)
+    atomicAdd(reinterpret_cast<unsigned long long*>(s.counters + kCtrSamples), my_samples);
+}
+
+constexpr int kOccThreads = 128;
+
+__global__ void __launch_bounds__(kOccThreads)
+occupancy_kernel(const DevScene sc, float threshold, uint32_t* __restrict__ occ) {
+  extern __shared__ float4 smem_raw[];
+  SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
+  load_weights32(W, sc.weights);
+  __syncthreads();
+  const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;  // grid covers 128^3 exactly
+  const uint32_t cx = cell % kOccRes, cy = (cell / kOccRes) % kOccRes, cz = cell / (kOccRes * kOccRes);
+  const float3 x = make_float3(((float)cx + 0.5f) / kOccRes, ((float)cy + 0.5f) / kOccRes,
+                               ((float)cz + 0.5f) / kOccRes);
+  float enc[kEnc];
+  encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
+  float dout[kDOut];
+  density_mlp32(W, enc, dout);
+  const float sigma = expf(dout[0] - 1.0f);
+  const unsigned bits = __ballot_sync(0xffffffffu, sigma > threshold);
+  if ((threadIdx.x & 31u) == 0) occ[cell >> 5] = bits;
+}
+
+__global__ void table_to_fp16_kernel(const float2* __restrict__ src, __half2* __restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = __float22half2_rn(src[i]);
+}
+
+}  // namespace
+
+cudaError_t launch_raygen(const ViewBatch& views, const DevScratch& s, cudaStream_t stream) {
+  if (views.total_pixels == 0) return cudaSuccess;
+  const unsigned blocks = (views.total_pixels + kRaygenThreads - 1) / kRaygenThreads;
+  raygen_kernel<<<blocks, kRaygenThreads, 0, stream>>>(views, s.ray_dt, s.ray_meta, s.counters, s.max_rays);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_march_fp32(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
+                              int num_sms, cudaStream_t stream) {
+  const int smem = (int)sizeof(SmemWeights32);
+  static bool attr_set = false;  // idempotent; harmless if two threads race on it
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(march_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_fp32_kernel, kMarchThreads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  march_fp32_kernel<<<num_sms * per_sm, kMarchThreads, smem, stream>>>(views, scene, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_occupancy(const DevScene& scene, float threshold, uint32_t* occ_out, cudaStream_t stream) {
+  const int smem = (int)sizeof(SmemWeights32);
+  cudaError_t e = cudaFuncSetAttribute(occupancy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const unsigned cells = kOccRes * kOccRes * kOccRes;
+  occupancy_kernel<<<cells / kOccThreads, kOccThreads, smem, stream>>>(scene, threshold, occ_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_table_to_fp16(const float2* src, __half2* dst, size_t n, cudaStream_t stream) {
+  table_to_fp16_kernel<<<1024, 256, 0, stream>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+}  // namespace nes

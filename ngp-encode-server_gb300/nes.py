@@ -1,0 +1,327 @@
+"""ctypes binding of libnes_gb300.so (the C ABI in include/nes_gb300.h).
+
+This is the host-side mirror a Python caller (tests, the benchmark, a
+serving driver) uses.  It adds no compute of its own: every call goes through
+the CUDA library, and loading fails loudly when the library is missing.
+
+Reference interfaces mirrored:
+  - Renderer.render(request_bytes) -> RenderedFrame bytes: the renderer round
+    trip of src/server.cpp:161-194 (FrameRequest out, RenderedFrame back).
+  - rgb24_to_yuv420p / gray8_to_yuv420p: RenderedFrame::convert_frame
+    (include/base/video/rendered_frame.h:24-33).
+Errors: negative errno-style codes, raised as NesError (the reference returns
+-errno from its socket helpers, src/server.cpp:23-43, and throws
+std::runtime_error from the receive path, src/server.cpp:91-112).
+"""
+import ctypes
+import math
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnes_gb300.so")
+HEADER = os.path.normpath(os.path.join(HERE, "..", "include", "nes_gb300.h"))
+
+NES_OK = 0
+NES_EIO = -5
+NES_EAGAIN = -11
+NES_ENOMEM = -12
+NES_ENODEV = -19
+NES_EINVAL = -22
+NES_EPROTO = -71
+NES_ENOBUFS = -105
+NES_ETIMEDOUT = -110
+
+PREC_FP32 = 0
+PREC_FP16_TC = 1
+
+
+class NesError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        super().__init__("%s: %s (%d)" % (what, _strerror(code), code))
+
+
+class NesConfig(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("log2_table_size", ctypes.c_uint32),
+                ("precision", ctypes.c_int32), ("fov_deg", ctypes.c_float),
+                ("depth_gray_max", ctypes.c_float), ("device", ctypes.c_int32),
+                ("max_pixels", ctypes.c_uint32)]
+
+
+class NesView(ctypes.Structure):
+    _fields_ = [("matrix", ctypes.c_float * 12), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("focal_px", ctypes.c_float),
+                ("flags", ctypes.c_uint32)]
+
+
+class NesFrameRequest(ctypes.Structure):
+    _fields_ = [("index", ctypes.c_uint64), ("is_left", ctypes.c_int32),
+                ("has_camera", ctypes.c_int32),
+                ("camera_is_left", ctypes.c_int32), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("matrix_len", ctypes.c_uint32),
+                ("matrix", ctypes.c_float * 12)]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_SZ = ctypes.c_size_t
+_SIGS = {
+    "nes_config_default": (None, [ctypes.POINTER(NesConfig)]),
+    "nes_create": (_I, [ctypes.POINTER(NesConfig), ctypes.POINTER(_P)]),
+    "nes_destroy": (None, [_P]),
+    "nes_strerror": (ctypes.c_char_p, [_I]),
+    "nes_focal_from_fov": (ctypes.c_float, [ctypes.c_uint32, ctypes.c_float]),
+    "nes_rendered_frame_capacity": (_SZ, [ctypes.c_uint32, ctypes.c_uint32]),
+    "nes_render": (_I, [_P, _P, _SZ, _P, _SZ, ctypes.POINTER(_SZ)]),
+    "nes_render_views": (_I, [_P, _P, _I, _P, _P, _P]),
+    "nes_render_yuv": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(_I), _P]),
+    "nes_rgb24_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
+    "nes_gray8_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
+    "nes_depth_pack_u16mm": (_I, [_P, _SZ, _P, _P]),
+    "nes_depth_to_gray8": (_I, [_P, _SZ, ctypes.c_float, _P, _P]),
+    "nes_rgb_to_rgb24": (_I, [_P, _SZ, _P, _P]),
+    "nes_scene_param": (_I, [_P, _I, _P, _SZ]),
+    "nes_occupancy": (_I, [_P, _P]),
+    "nes_rebuild_occupancy": (_I, [_P, ctypes.c_float]),
+    "nes_last_sample_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    "nes_set_profiling": (_I, [_P, _I]),
+    "nes_last_timings": (_I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "nes_scene_generate": (_I, [ctypes.c_uint64, ctypes.c_uint32, _P, _P]),
+    "nes_parse_frame_request": (_I, [_P, _SZ, ctypes.POINTER(NesFrameRequest)]),
+    "nes_write_rendered_frame": (_I, [ctypes.POINTER(NesFrameRequest), _P, _SZ, _P, _SZ,
+                                      _P, _SZ, ctypes.POINTER(_SZ)]),
+}
+
+_lib = None
+
+
+def header_symbols():
+    """Names of every function declared in include/nes_gb300.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nes_[a-z0-9_]+)\s*\(", text)))
+
+
+def load(path=None):
+    """Loads the CUDA library; raises OSError when it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    lib = ctypes.CDLL(path or LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _strerror(code):
+    try:
+        return load().nes_strerror(code).decode()
+    except OSError:
+        return "error"
+
+
+def check(rc, what):
+    if rc != NES_OK:
+        raise NesError(rc, what)
+
+
+def focal_from_fov(width, fov_deg):
+    return load().nes_focal_from_fov(width, fov_deg)
+
+
+def make_view(matrix, width, height, focal):
+    v = NesView()
+    for i in range(12):
+        v.matrix[i] = float(matrix[i])
+    v.width = width
+    v.height = height
+    v.focal_px = focal
+    v.flags = 0
+    return v
+
+
+def default_config(**kw):
+    cfg = NesConfig()
+    load().nes_config_default(ctypes.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def linesizes(width, align=32):
+    """av_image_alloc-style YUV420P linesizes (FrameManager aligns to 32,
+    include/base/video/type_managers.h:164)."""
+    cw = (width + 1) // 2
+    a = lambda x: (x + align - 1) // align * align
+    return [a(width), a(cw), a(cw)]
+
+
+class Renderer:
+    """One rendering context (scene + device buffers) on one GPU."""
+
+    def __init__(self, **kw):
+        self.lib = load()
+        self.cfg = default_config(**kw)
+        h = _P()
+        check(self.lib.nes_create(ctypes.byref(self.cfg), ctypes.byref(h)), "nes_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.nes_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def render(self, request: bytes) -> bytes:
+        """FrameRequest bytes -> RenderedFrame bytes (wire-compatible)."""
+        n = _SZ(0)
+        buf = ctypes.create_string_buffer(request, len(request))
+        rc = self.lib.nes_render(self.h, buf, len(request), None, 0, ctypes.byref(n))
+        if rc not in (NES_OK, NES_ENOBUFS):
+            raise NesError(rc, "nes_render")
+        out = ctypes.create_string_buffer(n.value)
+        check(self.lib.nes_render(self.h, buf, len(request), out, n.value, ctypes.byref(n)),
+              "nes_render")
+        return out.raw[:n.value]
+
+    def render_views(self, views, rgb_ptrs, depth_ptrs, stream=0):
+        nv = len(views)
+        arr = (NesView * nv)(*views)
+        rgb = (_P * nv)(*[p or None for p in rgb_ptrs]) if rgb_ptrs is not None else None
+        dep = (_P * nv)(*[p or None for p in depth_ptrs]) if depth_ptrs is not None else None
+        check(self.lib.nes_render_views(self.h, arr, nv, rgb, dep, _P(stream) if stream else None),
+              "nes_render_views")
+
+    def render_yuv(self, view, y_ptr, u_ptr, v_ptr, ls, depth_ptr=None):
+        lsa = (_I * 3)(*ls)
+        check(self.lib.nes_render_yuv(self.h, ctypes.byref(view), _P(y_ptr), _P(u_ptr), _P(v_ptr), lsa,
+                                      _P(depth_ptr) if depth_ptr else None), "nes_render_yuv")
+
+    def scene_param(self, which, count):
+        import numpy as np
+        out = np.empty(count, dtype=np.float32)
+        check(self.lib.nes_scene_param(self.h, which, out.ctypes.data, count), "nes_scene_param")
+        return out
+
+    def occupancy(self):
+        import numpy as np
+        out = np.empty(65536, dtype=np.uint32)
+        check(self.lib.nes_occupancy(self.h, out.ctypes.data), "nes_occupancy")
+        return out
+
+    def rebuild_occupancy(self, threshold):
+        check(self.lib.nes_rebuild_occupancy(self.h, threshold), "nes_rebuild_occupancy")
+
+    def last_sample_count(self):
+        v = ctypes.c_uint64(0)
+        check(self.lib.nes_last_sample_count(self.h, ctypes.byref(v)), "nes_last_sample_count")
+        return v.value
+
+    def set_profiling(self, on=True):
+        check(self.lib.nes_set_profiling(self.h, 1 if on else 0), "nes_set_profiling")
+
+    def last_timings(self):
+        """(raygen_ms, march_ms) of the last render, from CUDA events."""
+        a, b = ctypes.c_float(0), ctypes.c_float(0)
+        check(self.lib.nes_last_timings(self.h, ctypes.byref(a), ctypes.byref(b)), "nes_last_timings")
+        return a.value, b.value
+
+
+def rgb24_to_yuv420p(rgb_ptr, w, h, rgb_ls, y, u, v, ls, stream=0):
+    lsa = (_I * 3)(*ls)
+    check(load().nes_rgb24_to_yuv420p(_P(rgb_ptr), w, h, rgb_ls, _P(y), _P(u), _P(v), lsa,
+                                      _P(stream) if stream else None), "nes_rgb24_to_yuv420p")
+
+
+def gray8_to_yuv420p(g_ptr, w, h, g_ls, y, u, v, ls, stream=0):
+    lsa = (_I * 3)(*ls)
+    check(load().nes_gray8_to_yuv420p(_P(g_ptr), w, h, g_ls, _P(y), _P(u), _P(v), lsa,
+                                      _P(stream) if stream else None), "nes_gray8_to_yuv420p")
+
+
+def depth_pack_u16mm(d_ptr, n, out_ptr, stream=0):
+    check(load().nes_depth_pack_u16mm(_P(d_ptr), n, _P(out_ptr), _P(stream) if stream else None),
+          "nes_depth_pack_u16mm")
+
+
+def scene_generate(seed, log2T):
+    """Host-side scene generation (no GPU): (table, weights) as numpy."""
+    import numpy as np
+    T = 1 << log2T
+    table = np.empty(16 * T * 2, dtype=np.float32)
+    weights = np.empty(9408, dtype=np.float32)
+    check(load().nes_scene_generate(seed, log2T, table.ctypes.data, weights.ctypes.data),
+          "nes_scene_generate")
+    return table, weights
+
+
+# ---------------------------------------------------------------------------
+# Poses (host side).  SplitMix64 stream 6 of the workload seed: pose k uses
+# draws 3k, 3k+1, 3k+2 for z = 1 - 2u, phi = 2 pi u, r = rmin + (rmax-rmin) u;
+# the eye sits at centre + r * (sqrt(1-z^2) cos phi, sqrt(1-z^2) sin phi, z)
+# looking at the cube centre (0.5, 0.5, 0.5).
+# ---------------------------------------------------------------------------
+_M64 = (1 << 64) - 1
+
+
+def _mix64(z):
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+    return z ^ (z >> 31)
+
+
+def _u01(key, i):
+    return (_mix64((key + (i + 1) * 0x9E3779B97F4A7C15) & _M64) >> 11) * 2.0 ** -53
+
+
+def look_at(eye, centre=(0.5, 0.5, 0.5)):
+    """3x4 row-major pose: columns right, down, forward, eye."""
+    f = [centre[i] - eye[i] for i in range(3)]
+    n = math.sqrt(sum(v * v for v in f))
+    f = [v / n for v in f]
+    up = (0.0, 0.0, 1.0) if abs(f[2]) < 0.99 else (0.0, 1.0, 0.0)
+    r = [f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]]
+    n = math.sqrt(sum(v * v for v in r))
+    r = [v / n for v in r]
+    d = [f[1] * r[2] - f[2] * r[1], f[2] * r[0] - f[0] * r[2], f[0] * r[1] - f[1] * r[0]]
+    return [r[0], d[0], f[0], eye[0], r[1], d[1], f[1], eye[1], r[2], d[2], f[2], eye[2]]
+
+
+def shell_poses(seed, count, rmin, rmax, centre=(0.5, 0.5, 0.5)):
+    key = _mix64((seed * 256 + 6) & _M64)
+    out = []
+    for k in range(count):
+        z = 1.0 - 2.0 * _u01(key, 3 * k)
+        phi = 2.0 * math.pi * _u01(key, 3 * k + 1)
+        r = rmin + (rmax - rmin) * _u01(key, 3 * k + 2)
+        s = math.sqrt(max(0.0, 1.0 - z * z))
+        eye = (centre[0] + r * s * math.cos(phi), centre[1] + r * s * math.sin(phi), centre[2] + r * z)
+        out.append(look_at(eye, centre))
+    return out
+
+
+def stereo_pair(pose, ipd):
+    """Left/right eye poses: the eye moves by -/+ ipd/2 along the right axis."""
+    out = []
+    for sgn in (-0.5, 0.5):
+        m = list(pose)
+        for row in range(3):
+            m[row * 4 + 3] = pose[row * 4 + 3] + sgn * ipd * pose[row * 4 + 0]
+        out.append(m)
+    return out

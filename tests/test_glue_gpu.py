@@ -1,0 +1,110 @@
+"""Frame glue on the GPU, bit-exact against the oracle's integer restatement
+(swscale itself is not installed anywhere this runs: swscale parity is
+unpinned).  Covers odd sizes, padded linesizes, the 1x1 frame, the configured
+frame sizes and depth-packing edge values."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def synth_frame(rng, w, h):
+    """50/50 blend of uniform bytes and a horizontal gradient."""
+    noise = rng.integers(0, 256, (h, w, 3)).astype(np.uint16)
+    grad = np.broadcast_to((np.arange(w) * 255 // max(1, w - 1)).astype(np.uint16)[None, :, None], (h, w, 3))
+    return ((noise + grad) // 2).astype(np.uint8)
+
+
+def gpu_yuv(torch, nes_lib, img, w, h, rgb_ls, ls, gray=False):
+    ch = (h + 1) // 2
+    src = torch.from_numpy(np.ascontiguousarray(img).reshape(-1)).cuda()
+    y = torch.full((ls[0] * h,), 7, dtype=torch.uint8, device="cuda")
+    u = torch.full((ls[1] * ch,), 7, dtype=torch.uint8, device="cuda")
+    v = torch.full((ls[2] * ch,), 7, dtype=torch.uint8, device="cuda")
+    fn = nes_lib.gray8_to_yuv420p if gray else nes_lib.rgb24_to_yuv420p
+    fn(src.data_ptr(), w, h, rgb_ls, y.data_ptr(), u.data_ptr(), v.data_ptr(), ls)
+    torch.cuda.synchronize()
+    return y.cpu().numpy(), u.cpu().numpy(), v.cpu().numpy()
+
+
+def visible(plane, ls, w, h):
+    return plane.reshape(-1, ls)[:h, :w]
+
+
+@pytest.mark.parametrize("w,h,pad", [(1280, 720, 0), (1920, 1080, 0), (1920, 1832, 0), (640, 360, 0),
+                                      (33, 17, 0), (31, 1, 5), (1, 1, 0), (2, 2, 3), (257, 255, 32)])
+def test_rgb24_to_yuv420p_bit_exact(cuda, nes_lib, oracle_mod, w, h, pad):
+    rng = np.random.default_rng(w * 7919 + h)
+    img = synth_frame(rng, w, h)
+    rgb_ls = 3 * w + pad
+    buf = np.zeros((h, rgb_ls), np.uint8)
+    buf[:, :3 * w] = img.reshape(h, 3 * w)
+    ls = nes_lib.linesizes(w)
+    gy, gu, gv = gpu_yuv(cuda, nes_lib, buf, w, h, rgb_ls, ls)
+    oy, ou, ov = oracle_mod.rgb24_to_yuv420p(buf, w, h, rgb_ls, ls)
+    cw, ch = (w + 1) // 2, (h + 1) // 2
+    assert np.array_equal(visible(gy, ls[0], w, h), visible(oy, ls[0], w, h))
+    assert np.array_equal(visible(gu, ls[1], cw, ch), visible(ou, ls[1], cw, ch))
+    assert np.array_equal(visible(gv, ls[2], cw, ch), visible(ov, ls[2], cw, ch))
+    # Padding bytes past each row's width are left untouched.
+    if ls[0] > w:
+        assert np.all(gy.reshape(-1, ls[0])[:, w:] == 7)
+
+
+def test_golden_yuv_on_gpu(cuda, nes_lib):
+    g = np.load(os.path.join(GOLDEN, "yuv_small.npz"))
+    w, h, ls = int(g["w"]), int(g["h"]), [int(v) for v in g["ls"]]
+    y, u, v = gpu_yuv(cuda, nes_lib, g["rgb"], w, h, w * 3, ls)
+    cw, ch = (w + 1) // 2, (h + 1) // 2
+    assert np.array_equal(visible(y, ls[0], w, h), visible(g["y"], ls[0], w, h))
+    assert np.array_equal(visible(u, ls[1], cw, ch), visible(g["u"], ls[1], cw, ch))
+    assert np.array_equal(visible(v, ls[2], cw, ch), visible(g["v"], ls[2], cw, ch))
+
+
+@pytest.mark.parametrize("w,h", [(1280, 720), (33, 17), (1, 1)])
+def test_gray8_to_yuv420p_bit_exact(cuda, nes_lib, oracle_mod, w, h):
+    rng = np.random.default_rng(w + h)
+    g = rng.integers(0, 256, (h, w), dtype=np.uint8)
+    ls = nes_lib.linesizes(w)
+    gy, gu, gv = gpu_yuv(cuda, nes_lib, g, w, h, w, ls, gray=True)
+    oy, ou, ov = oracle_mod.gray8_to_yuv420p(g, w, h, w, ls)
+    cw, ch = (w + 1) // 2, (h + 1) // 2
+    assert np.array_equal(visible(gy, ls[0], w, h), visible(oy, ls[0], w, h))
+    assert np.array_equal(visible(gu, ls[1], cw, ch), visible(ou, ls[1], cw, ch))
+
+
+def test_depth_pack_bit_exact(cuda, nes_lib, oracle_mod):
+    torch = cuda
+    rng = np.random.default_rng(0)
+    d = np.concatenate([rng.uniform(0.1, 10.0, 1280 * 720 * 30 // 16).astype(np.float32),
+                        np.array([0.0, 0.0004, 0.0005, 1.2345, 65.5349, 65.535, 1e9, -1.0, np.nan, np.inf,
+                                  -np.inf, -0.0], np.float32)])
+    src = torch.from_numpy(d).cuda()
+    out = torch.empty(d.size, dtype=torch.int16, device="cuda")
+    nes_lib.depth_pack_u16mm(src.data_ptr(), d.size, out.data_ptr())
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint16)
+    assert np.array_equal(got, oracle_mod.depth_pack_u16mm(d))
+
+
+def test_rgb24_and_gray8_quantisation(cuda, nes_lib, oracle_mod):
+    torch = cuda
+    lib = nes_lib.load()
+    rng = np.random.default_rng(1)
+    x = np.concatenate([rng.uniform(-0.2, 1.2, 100000), np.arange(256) / 255.0, [0.5 / 255, 1.5 / 255]])
+    x = x.astype(np.float32)
+    src = torch.from_numpy(x).cuda()
+    out = torch.empty(x.size, dtype=torch.uint8, device="cuda")
+    assert lib.nes_rgb_to_rgb24(src.data_ptr(), x.size, out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), oracle_mod.rgb_to_rgb24(x))
+    d = rng.uniform(-1, 6, 50000).astype(np.float32)
+    src = torch.from_numpy(d).cuda()
+    out = torch.empty(d.size, dtype=torch.uint8, device="cuda")
+    assert lib.nes_depth_to_gray8(src.data_ptr(), d.size, 4.0, out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), oracle_mod.depth_to_gray8(d, 4.0))

@@ -1,0 +1,134 @@
+"""GPU render parity: the CUDA march against the FP64 oracle on the same
+seeded scene.  Tolerances (from the spec of this path): PSNR >= 45 dB on
+RGB in [0,1] and max |delta depth| <= 1e-3 of the unit-cube extent; the
+integer sample count per frame must match the oracle exactly (the ray set-up
+is FP32-exact on both sides)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PSNR_MIN = 45.0
+DEPTH_TOL = 1e-3
+
+
+def render_gpu(r, torch, views):
+    """views: list of (matrix, W, H, focal) -> list of (rgb[H*W,3], depth[H*W])."""
+    import nes
+    vs, rgbs, deps = [], [], []
+    for (M, W, H, f) in views:
+        vs.append(nes.make_view(M, W, H, f))
+        rgbs.append(torch.full((H * W, 3), -1.0, device="cuda", dtype=torch.float32))
+        deps.append(torch.full((H * W,), -1.0, device="cuda", dtype=torch.float32))
+    r.render_views(vs, [t.data_ptr() for t in rgbs], [t.data_ptr() for t in deps])
+    torch.cuda.synchronize()
+    return [(a.cpu().numpy(), b.cpu().numpy()) for a, b in zip(rgbs, deps)]
+
+
+def psnr(a, b):
+    import oracle
+    return oracle.psnr(a, b)
+
+
+POSES = {
+    "sphere0": lambda nes: nes.shell_poses(0, 3, 1.5, 1.5)[0],
+    "sphere2": lambda nes: nes.shell_poses(0, 3, 1.5, 1.5)[2],
+    "shell": lambda nes: nes.shell_poses(9, 1, 1.2, 2.0)[0],
+    "inside": lambda nes: [1, 0, 0, .5, 0, -1, 0, .5, 0, 0, -1, .5],  # camera_manager.h:18-19
+}
+
+
+@pytest.mark.parametrize("pose", sorted(POSES))
+def test_fp32_full_view_vs_oracle(r32, cuda, scene0, nes_lib, pose):
+    M = POSES[pose](nes_lib)
+    W, H = 48, 40
+    f = nes_lib.focal_from_fov(W, 90.0)
+    (rgb, dep), = render_gpu(r32, cuda, [(M, W, H, f)])
+    gpu_samples = r32.last_sample_count()
+    orgb, odep, osamples = scene0.render(M, W, H, f)
+    assert gpu_samples == osamples
+    assert psnr(rgb, orgb) >= PSNR_MIN
+    assert np.abs(dep - odep).max() <= DEPTH_TOL
+    # FP32 plain path is far tighter than the spec tolerance.
+    assert np.abs(rgb - orgb).max() < 1e-4
+
+
+def test_fp32_1080p_pixel_subset_vs_oracle(r32, cuda, scene0, nes_lib):
+    M = nes_lib.shell_poses(0, 100, 1.5, 1.5)[17]
+    W, H = 1920, 1080
+    f = nes_lib.focal_from_fov(W, 90.0)
+    (rgb, dep), = render_gpu(r32, cuda, [(M, W, H, f)])
+    rng = np.random.default_rng(5)
+    pix = rng.choice(W * H, 3000, replace=False).astype(np.int32)
+    orgb, odep, _ = scene0.render(M, W, H, f, pixels=pix)
+    assert psnr(rgb[pix], orgb) >= PSNR_MIN
+    assert np.abs(dep[pix] - odep).max() <= DEPTH_TOL
+
+
+def test_batched_views_equal_single_views(r32, cuda, nes_lib):
+    poses = nes_lib.shell_poses(4, 3, 1.2, 2.0)
+    views = [(poses[0], 64, 48, nes_lib.focal_from_fov(64, 90.0)),
+             (poses[1], 33, 17, nes_lib.focal_from_fov(33, 100.0))]
+    views += [(m, 40, 40, nes_lib.focal_from_fov(40, 100.0)) for m in nes_lib.stereo_pair(poses[2], 0.063)]
+    batched = render_gpu(r32, cuda, views)
+    for v, (rgb, dep) in zip(views, batched):
+        (rgb1, dep1), = render_gpu(r32, cuda, [v])
+        assert np.array_equal(rgb, rgb1) and np.array_equal(dep, dep1)
+
+
+def test_stereo_pair_vs_oracle(r32, cuda, scene0, nes_lib):
+    pose = nes_lib.shell_poses(2, 1, 1.2, 2.0)[0]
+    W, H = 40, 38
+    f = nes_lib.focal_from_fov(W, 100.0)
+    views = [(m, W, H, f) for m in nes_lib.stereo_pair(pose, 0.063)]
+    out = render_gpu(r32, cuda, views)
+    for (M, _, _, _), (rgb, dep) in zip(views, out):
+        orgb, odep, _ = scene0.render(M, W, H, f)
+        assert psnr(rgb, orgb) >= PSNR_MIN
+        assert np.abs(dep - odep).max() <= DEPTH_TOL
+
+
+def test_occupancy_matches_oracle(r32, scene0):
+    bits = r32.occupancy()
+    assert np.array_equal(bits, scene0.occupancy())
+    # The seeded scene's density (~0.37) is far above 0.01 everywhere.
+    assert np.all(bits == 0xFFFFFFFF)
+
+
+def test_partial_occupancy_skips_cells(nes_lib, cuda, scene0):
+    """With a threshold near the median density the grid is partial; the
+    march must skip empty cells exactly like the oracle given the same grid."""
+    r = nes_lib.Renderer(precision=nes_lib.PREC_FP32, max_pixels=64 * 64)
+    try:
+        r.rebuild_occupancy(0.37)
+        bits = r.occupancy()
+        frac = np.unpackbits(bits.view(np.uint8)).mean()
+        assert 0.05 < frac < 0.95
+        obits = scene0.occupancy(threshold=0.37)
+        # Cells whose centre density sits within FP32 noise of the threshold
+        # may differ; there must be almost none.
+        assert np.count_nonzero(bits ^ obits) <= 8
+        M = nes_lib.shell_poses(0, 1, 1.5, 1.5)[0]
+        W = H = 48
+        f = nes_lib.focal_from_fov(W, 90.0)
+        (rgb, dep), = render_gpu(r, cuda, [(M, W, H, f)])
+        orgb, odep, _ = scene0.render(M, W, H, f, occ=bits)
+        assert psnr(rgb, orgb) >= PSNR_MIN
+        assert np.abs(dep - odep).max() <= DEPTH_TOL
+    finally:
+        r.close()
+
+
+def test_invalid_views_rejected(r32, nes_lib, cuda):
+    f = nes_lib.focal_from_fov(16, 90.0)
+    M = nes_lib.shell_poses(0, 1, 1.5, 1.5)[0]
+    with pytest.raises(nes_lib.NesError) as e:
+        r32.render_views([nes_lib.make_view(M, 0, 16, f)], [None], [None])
+    assert e.value.code == nes_lib.NES_EINVAL
+    with pytest.raises(nes_lib.NesError) as e:
+        r32.render_views([nes_lib.make_view(M, 16, 16, -1.0)], [None], [None])
+    assert e.value.code == nes_lib.NES_EINVAL
+    big = nes_lib.make_view(M, 4096, 4096, f)  # beyond max_pixels
+    with pytest.raises(nes_lib.NesError) as e:
+        r32.render_views([big], [None], [None])
+    assert e.value.code == nes_lib.NES_EINVAL

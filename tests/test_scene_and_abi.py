@@ -1,0 +1,99 @@
+"""Host-side checks that need no GPU: the product's scene generator against
+the oracle's independent one, the C ABI's exported symbols and argument
+validation, pose helpers."""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+
+@pytest.mark.parametrize("seed,log2T", [(0, 19), (0, 14), (1, 14), (2, 16)])
+def test_scene_generator_matches_oracle(nes_lib, oracle_mod, seed, log2T):
+    table, weights = nes_lib.scene_generate(seed, log2T)
+    s = oracle_mod.Scene(seed, log2T)
+    assert np.array_equal(table, s.param(0))
+    offs = [0, 2048, 3072, 5120, 9216, 9408]
+    for i in range(5):
+        assert np.array_equal(weights[offs[i]:offs[i + 1]], s.param(i + 1))
+
+
+def test_scene_value_ranges(nes_lib):
+    table, w = nes_lib.scene_generate(0, 14)
+    assert table.min() >= -0.5 and table.max() < 0.5
+    assert abs(float(table.mean())) < 0.01
+    a = math.sqrt(6 / (32 + 64))
+    assert np.abs(w[:2048]).max() <= a
+    cw1 = w[3072:5120].reshape(64, 32)
+    assert np.all(cw1[:, 31] == 0)
+
+
+def test_header_symbols_exported(nes_lib):
+    lib = nes_lib.load()
+    syms = nes_lib.header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), "missing export " + s
+
+
+def test_glue_rejects_bad_arguments_without_gpu(nes_lib):
+    lib = nes_lib.load()
+    ls = (ctypes.c_int * 3)(64, 32, 32)
+    assert lib.nes_rgb24_to_yuv420p(None, 64, 64, 192, None, None, None, ls, None) == nes_lib.NES_EINVAL
+    dummy = ctypes.c_void_p(16)
+    assert lib.nes_rgb24_to_yuv420p(dummy, 0, 64, 192, dummy, dummy, dummy, ls, None) == nes_lib.NES_EINVAL
+    bad = (ctypes.c_int * 3)(63, 32, 32)  # luma linesize below width
+    assert lib.nes_rgb24_to_yuv420p(dummy, 64, 64, 192, dummy, dummy, dummy, bad, None) == nes_lib.NES_EINVAL
+    assert lib.nes_depth_pack_u16mm(None, 10, None, None) == nes_lib.NES_EINVAL
+    assert lib.nes_depth_to_gray8(dummy, 10, 0.0, dummy, None) == nes_lib.NES_EINVAL
+    assert lib.nes_depth_pack_u16mm(None, 0, None, None) == nes_lib.NES_OK
+
+
+def test_create_validates_config(nes_lib):
+    lib = nes_lib.load()
+    h = ctypes.c_void_p()
+    cfg = nes_lib.default_config(log2_table_size=30)
+    assert lib.nes_create(ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
+    cfg = nes_lib.default_config(precision=7)
+    assert lib.nes_create(ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
+    cfg = nes_lib.default_config(fov_deg=180.0)
+    assert lib.nes_create(ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
+
+
+def test_create_without_gpu_fails_cleanly(nes_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(nes_lib.NesError) as e:
+        nes_lib.Renderer()
+    assert e.value.code == nes_lib.NES_ENODEV
+
+
+def test_focal_and_capacity(nes_lib):
+    assert nes_lib.focal_from_fov(1920, 90.0) == pytest.approx(960.0, rel=1e-6)
+    assert nes_lib.focal_from_fov(256, 90.0) == np.float32(128.0)
+    lib = nes_lib.load()
+    assert lib.nes_rendered_frame_capacity(1280, 720) >= 1280 * 720 * 4 + 32
+
+
+def test_poses_on_shell(nes_lib):
+    poses = nes_lib.shell_poses(0, 100, 1.5, 1.5)
+    for M in poses:
+        M = np.asarray(M).reshape(3, 4)
+        eye = M[:, 3]
+        assert abs(np.linalg.norm(eye - 0.5) - 1.5) < 1e-12
+        R = M[:, :3]
+        assert np.allclose(R.T @ R, np.eye(3), atol=1e-12)
+        # forward column looks at the centre
+        assert np.allclose(R[:, 2], (0.5 - eye) / 1.5, atol=1e-12)
+    shell = nes_lib.shell_poses(5, 200, 1.2, 2.0)
+    r = [np.linalg.norm(np.asarray(M).reshape(3, 4)[:, 3] - 0.5) for M in shell]
+    assert 1.2 <= min(r) and max(r) <= 2.0
+    left, right = nes_lib.stereo_pair(shell[0], 0.063)
+    assert abs(np.linalg.norm(np.asarray(left)[[3, 7, 11]] - np.asarray(right)[[3, 7, 11]]) - 0.063) < 1e-12
+
+
+def test_linesizes(nes_lib):
+    assert nes_lib.linesizes(1280) == [1280, 640, 640]
+    assert nes_lib.linesizes(1920) == [1920, 960, 960]
+    assert nes_lib.linesizes(33) == [64, 32, 32]
