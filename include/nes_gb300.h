@@ -121,6 +121,29 @@ int nes_render_views(nes_ctx *ctx, const nes_view *views, int nviews, float *con
 int nes_render_yuv(nes_ctx *ctx, const nes_view *view, uint8_t *y_host, uint8_t *u_host,
                    uint8_t *v_host, const int linesize[3], uint16_t *depth_mm_host);
 
+/* Largest view (width * height) nes_render_view_noalloc accepts. */
+#define NES_NOALLOC_MAX_PIXELS (1u << 18) /* 262,144 pixels, e.g. 512 x 512 */
+
+/* Plain FP32 render of one view that allocates no device memory.  No
+ * counterpart in the reference: it exists for callers that may not call
+ * cudaMalloc/cudaFree (a host application that owns all device memory and
+ * hands out fixed buffers, or a frame loop that cannot take the implicit
+ * synchronisation of an allocation).  The caller passes the scene
+ * (table_dev = 16 * 2^log2_table_size * 2 floats, weights_dev = the 9,408-float
+ * blob of nes_scene_generate, occupancy_dev = 65,536 words as nes_occupancy
+ * returns) and the outputs (rgb_dev W*H*3 floats, depth_dev W*H floats;
+ * either may be NULL).  Work is queued on `stream` (NULL = legacy default
+ * stream) on the calling thread's current device.  The ray list lives in a
+ * static device array of the library (8 MiB + 256 B, held by every GPU that
+ * loads the library's device code until exit): views above
+ * NES_NOALLOC_MAX_PIXELS pixels return NES_EINVAL.  All calls on a device
+ * share that array: calls whose GPU work overlaps race.  The first call on
+ * a device looks up the array's address (make it before any stream capture
+ * on that device). */
+int nes_render_view_noalloc(const float *table_dev, uint32_t log2_table_size, const float *weights_dev,
+                            const uint32_t *occupancy_dev, const nes_view *view, float *rgb_dev,
+                            float *depth_dev, void *stream);
+
 /* ---------------- (ii) frame glue ---------------- */
 
 /* RGB24 -> YUV420P, BT.601 studio range, 2x2 chroma average (edge pixels

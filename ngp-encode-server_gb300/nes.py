@@ -85,6 +85,7 @@ _SIGS = {
     "nes_occupancy": (_I, [_P, _P]),
     "nes_rebuild_occupancy": (_I, [_P, ctypes.c_float]),
     "nes_last_sample_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    "nes_render_view_noalloc": (_I, [_P, ctypes.c_uint32, _P, _P, ctypes.POINTER(NesView), _P, _P, _P]),
     "nes_set_profiling": (_I, [_P, _I]),
     "nes_last_timings": (_I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "nes_scene_generate": (_I, [ctypes.c_uint64, ctypes.c_uint32, _P, _P]),
