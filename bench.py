@@ -49,6 +49,8 @@ def parse_args():
     p.add_argument("--precision", choices=["auto", "fp32", "tc"], default="auto")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=None)
+    p.add_argument("--width", type=int, default=1920, help="smaller sizes only for profiling captures")
+    p.add_argument("--height", type=int, default=1080)
     return p.parse_args()
 
 
@@ -304,6 +306,10 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    global W, H, WORKLOAD
+    if (args.width, args.height) != (W, H):
+        W, H = args.width, args.height
+        WORKLOAD = WORKLOAD.replace("1920x1080", "%dx%d (profiling case)" % (W, H))
     if args.impl == "reference":
         run_reference(args)
     else:
