@@ -34,6 +34,7 @@ struct DevScratch {
 constexpr int kCtrRays = 0;
 constexpr int kCtrCursor = 1;
 constexpr int kCtrSamples = 2;  // 64-bit, occupies words 2 and 3
+constexpr int kCtrError = 4;    // nonzero: a bounded device wait ran out
 constexpr int kCtrWords = 8;
 
 // Ray generation + unit-cube clip + warp-ballot compaction of hits; writes
@@ -45,9 +46,14 @@ cudaError_t launch_raygen(const ViewBatch& views, const DevScratch& s, cudaStrea
 cudaError_t launch_march_fp32(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
                               int num_sms, cudaStream_t stream);
 
-// FP16 tensor-core march (tcgen05 MLP).
+// FP16 tensor-core march (tcgen05 MLP).  Needs scene.table16 and
+// scene.tc_weights (the FP16 operand image from launch_pack_tc_weights).
 cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
                             int num_sms, cudaStream_t stream);
+
+// Bytes of the FP16 MLP weight image and its packing from the FP32 blob.
+size_t tc_weight_bytes();
+cudaError_t launch_pack_tc_weights(const float* w32, uint8_t* out, cudaStream_t stream);
 
 // 128^3 occupancy bitfield from the FP32 density at cell centres.
 cudaError_t launch_occupancy(const DevScene& scene, float threshold, uint32_t* occ_out,

@@ -47,12 +47,6 @@ struct nes_ctx {
   cudaEvent_t ev_t[3] = {nullptr, nullptr, nullptr};
 };
 
-// Tensor-core weight packing lives with the tensor-core kernel.
-namespace nes {
-size_t tc_weight_bytes();
-void pack_tc_weights(const float* w32, uint8_t* out);
-}  // namespace nes
-
 namespace {
 
 #define NES_CUDA(call)                        \
@@ -110,6 +104,17 @@ int render_batch_locked(nes_ctx* c, const nes_view* views, int n, float* const* 
   }
   c->samples_pending = true;
   return NES_OK;
+}
+
+// After the stream is idle: reads the last render's sample count and the
+// device error word (set when a bounded wait inside a kernel ran out).
+int collect_status(nes_ctx* c) {
+  if (!c->samples_pending) return NES_OK;
+  uint32_t w[3] = {0, 0, 0};  // samples lo, samples hi, error
+  NES_CUDA(cudaMemcpy(w, c->scratch.counters + kCtrSamples, sizeof(w), cudaMemcpyDeviceToHost));
+  c->last_samples = (uint64_t)w[0] | ((uint64_t)w[1] << 32);
+  c->samples_pending = false;
+  return w[2] ? NES_ETIMEDOUT : NES_OK;
 }
 
 // Runs fn on ctx->stream ordered after everything already queued on `user`
@@ -239,11 +244,8 @@ int nes_create(const nes_config* cfg, nes_ctx** out) {
   if (cfg->precision == NES_PREC_FP16_TC) {
     if ((rc = dalloc(&c->d_table16, entries)) != NES_OK) return fail(rc);
     if (launch_table_to_fp16(c->d_table32, c->d_table16, entries, c->stream) != cudaSuccess) return fail(NES_EIO);
-    std::vector<uint8_t> packed(tc_weight_bytes());
-    pack_tc_weights(host.weights.data(), packed.data());
-    if ((rc = dalloc(&c->d_tc_weights, packed.size())) != NES_OK) return fail(rc);
-    if (cudaMemcpy(c->d_tc_weights, packed.data(), packed.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-      return fail(NES_EIO);
+    if ((rc = dalloc(&c->d_tc_weights, tc_weight_bytes())) != NES_OK) return fail(rc);
+    if (launch_pack_tc_weights(c->d_weights, c->d_tc_weights, c->stream) != cudaSuccess) return fail(NES_EIO);
     c->scene.table16 = c->d_table16;
     c->scene.tc_weights = c->d_tc_weights;
   }
@@ -309,7 +311,7 @@ int nes_render(nes_ctx* c, const uint8_t* request, size_t request_len, uint8_t* 
   NES_CUDA(cudaMemcpyAsync(frame_out + L.frame_offset, c->d_rgb8, px * 3, cudaMemcpyDeviceToHost, c->stream));
   NES_CUDA(cudaMemcpyAsync(frame_out + L.depth_offset, c->d_gray, px, cudaMemcpyDeviceToHost, c->stream));
   NES_CUDA(cudaStreamSynchronize(c->stream));
-  return NES_OK;
+  return collect_status(c);
 }
 
 int nes_render_views(nes_ctx* c, const nes_view* views, int nviews, float* const* rgb_dev,
@@ -347,7 +349,7 @@ int nes_render_yuv(nes_ctx* c, const nes_view* view, uint8_t* y_host, uint8_t* u
   if (depth_mm_host)
     NES_CUDA(cudaMemcpyAsync(depth_mm_host, c->d_depth16, px * sizeof(uint16_t), cudaMemcpyDeviceToHost, c->stream));
   NES_CUDA(cudaStreamSynchronize(c->stream));
-  return NES_OK;
+  return collect_status(c);
 }
 
 int nes_rgb24_to_yuv420p(const uint8_t* rgb_dev, int width, int height, int rgb_linesize, uint8_t* y_dev,
@@ -471,22 +473,17 @@ int nes_rebuild_occupancy(nes_ctx* c, float threshold) {
   NES_CUDA(cudaSetDevice(c->cfg.device));
   NES_CUDA(launch_occupancy(c->scene, threshold, c->d_occ, c->stream));
   NES_CUDA(cudaStreamSynchronize(c->stream));
-  return NES_OK;
+  return collect_status(c);
 }
 
 int nes_last_sample_count(nes_ctx* c, uint64_t* samples) {
   if (!c || !samples) return NES_EINVAL;
   std::lock_guard<std::mutex> lock(c->mu);
   NES_CUDA(cudaSetDevice(c->cfg.device));
-  if (c->samples_pending) {
-    NES_CUDA(cudaStreamSynchronize(c->stream));
-    unsigned long long v = 0;
-    NES_CUDA(cudaMemcpy(&v, c->scratch.counters + kCtrSamples, sizeof(v), cudaMemcpyDeviceToHost));
-    c->last_samples = v;
-    c->samples_pending = false;
-  }
+  NES_CUDA(cudaStreamSynchronize(c->stream));
+  const int rc = collect_status(c);
   *samples = c->last_samples;
-  return NES_OK;
+  return rc;
 }
 
 int nes_set_profiling(nes_ctx* c, int enable) {

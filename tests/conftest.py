@@ -53,3 +53,17 @@ def r32(nes_lib, cuda):
     r = nes_lib.Renderer(precision=nes_lib.PREC_FP32, max_pixels=2 * 1920 * 1832)
     yield r
     r.close()
+
+
+@pytest.fixture(scope="session")
+def rtc(nes_lib, cuda):
+    """FP16 tensor-core renderer on the reference scene (seed 0, 2^19)."""
+    r = nes_lib.Renderer(precision=nes_lib.PREC_FP16_TC, max_pixels=2 * 1920 * 1832)
+    yield r
+    r.close()
+
+
+@pytest.fixture(params=["fp32", "tc"])
+def renderer(request, nes_lib, cuda):
+    """Both precisions of the reference-scene renderer."""
+    return request.getfixturevalue("r32" if request.param == "fp32" else "rtc")

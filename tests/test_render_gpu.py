@@ -39,25 +39,26 @@ POSES = {
 
 
 @pytest.mark.parametrize("pose", sorted(POSES))
-def test_fp32_full_view_vs_oracle(r32, cuda, scene0, nes_lib, pose):
+def test_full_view_vs_oracle(renderer, cuda, scene0, nes_lib, pose):
     M = POSES[pose](nes_lib)
     W, H = 48, 40
     f = nes_lib.focal_from_fov(W, 90.0)
-    (rgb, dep), = render_gpu(r32, cuda, [(M, W, H, f)])
-    gpu_samples = r32.last_sample_count()
+    (rgb, dep), = render_gpu(renderer, cuda, [(M, W, H, f)])
+    gpu_samples = renderer.last_sample_count()
     orgb, odep, osamples = scene0.render(M, W, H, f)
     assert gpu_samples == osamples
     assert psnr(rgb, orgb) >= PSNR_MIN
     assert np.abs(dep - odep).max() <= DEPTH_TOL
-    # FP32 plain path is far tighter than the spec tolerance.
-    assert np.abs(rgb - orgb).max() < 1e-4
+    if renderer.cfg.precision == nes_lib.PREC_FP32:
+        # The plain FP32 path is far tighter than the spec tolerance.
+        assert np.abs(rgb - orgb).max() < 1e-4
 
 
-def test_fp32_1080p_pixel_subset_vs_oracle(r32, cuda, scene0, nes_lib):
+def test_1080p_pixel_subset_vs_oracle(renderer, cuda, scene0, nes_lib):
     M = nes_lib.shell_poses(0, 100, 1.5, 1.5)[17]
     W, H = 1920, 1080
     f = nes_lib.focal_from_fov(W, 90.0)
-    (rgb, dep), = render_gpu(r32, cuda, [(M, W, H, f)])
+    (rgb, dep), = render_gpu(renderer, cuda, [(M, W, H, f)])
     rng = np.random.default_rng(5)
     pix = rng.choice(W * H, 3000, replace=False).astype(np.int32)
     orgb, odep, _ = scene0.render(M, W, H, f, pixels=pix)
@@ -65,27 +66,75 @@ def test_fp32_1080p_pixel_subset_vs_oracle(r32, cuda, scene0, nes_lib):
     assert np.abs(dep[pix] - odep).max() <= DEPTH_TOL
 
 
-def test_batched_views_equal_single_views(r32, cuda, nes_lib):
+def test_batched_views_equal_single_views(renderer, cuda, nes_lib):
     poses = nes_lib.shell_poses(4, 3, 1.2, 2.0)
     views = [(poses[0], 64, 48, nes_lib.focal_from_fov(64, 90.0)),
              (poses[1], 33, 17, nes_lib.focal_from_fov(33, 100.0))]
     views += [(m, 40, 40, nes_lib.focal_from_fov(40, 100.0)) for m in nes_lib.stereo_pair(poses[2], 0.063)]
-    batched = render_gpu(r32, cuda, views)
+    batched = render_gpu(renderer, cuda, views)
     for v, (rgb, dep) in zip(views, batched):
-        (rgb1, dep1), = render_gpu(r32, cuda, [v])
+        (rgb1, dep1), = render_gpu(renderer, cuda, [v])
         assert np.array_equal(rgb, rgb1) and np.array_equal(dep, dep1)
 
 
-def test_stereo_pair_vs_oracle(r32, cuda, scene0, nes_lib):
+def test_stereo_pair_vs_oracle(renderer, cuda, scene0, nes_lib):
     pose = nes_lib.shell_poses(2, 1, 1.2, 2.0)[0]
     W, H = 40, 38
     f = nes_lib.focal_from_fov(W, 100.0)
     views = [(m, W, H, f) for m in nes_lib.stereo_pair(pose, 0.063)]
-    out = render_gpu(r32, cuda, views)
+    out = render_gpu(renderer, cuda, views)
     for (M, _, _, _), (rgb, dep) in zip(views, out):
         orgb, odep, _ = scene0.render(M, W, H, f)
         assert psnr(rgb, orgb) >= PSNR_MIN
         assert np.abs(dep - odep).max() <= DEPTH_TOL
+
+
+def test_stereo_1832_pixel_subset_vs_oracle(rtc, cuda, scene0, nes_lib):
+    """The precision-form workload: a stereo pair of 1920x1832 views at
+    100 deg FOV from the r = 1.2..2.0 shell, IPD 0.063, on the tensor cores."""
+    pose = nes_lib.shell_poses(0, 200, 1.2, 2.0)[11]
+    W, H = 1920, 1832
+    f = nes_lib.focal_from_fov(W, 100.0)
+    views = [(m, W, H, f) for m in nes_lib.stereo_pair(pose, 0.063)]
+    out = render_gpu(rtc, cuda, views)
+    rng = np.random.default_rng(8)
+    for (M, _, _, _), (rgb, dep) in zip(views, out):
+        pix = rng.choice(W * H, 2000, replace=False).astype(np.int32)
+        orgb, odep, _ = scene0.render(M, W, H, f, pixels=pix)
+        assert psnr(rgb[pix], orgb) >= PSNR_MIN
+        assert np.abs(dep[pix] - odep).max() <= DEPTH_TOL
+
+
+@pytest.mark.parametrize("log2T", [14, 22])
+def test_table_size_sweep_vs_oracle(nes_lib, oracle_mod, cuda, log2T):
+    """Hash-table sizes 2^14 (more collisions, fewer dense levels) and 2^22
+    (eight dense levels), tensor-core path, against the oracle."""
+    scene = oracle_mod.Scene(0, log2T)
+    M = nes_lib.shell_poses(1, 1, 1.5, 1.5)[0]
+    W, H = 40, 32
+    f = nes_lib.focal_from_fov(W, 90.0)
+    for prec in (nes_lib.PREC_FP16_TC, nes_lib.PREC_FP32):
+        r = nes_lib.Renderer(precision=prec, log2_table_size=log2T, max_pixels=W * H)
+        try:
+            (rgb, dep), = render_gpu(r, cuda, [(M, W, H, f)])
+            samples = r.last_sample_count()
+        finally:
+            r.close()
+        orgb, odep, osamples = scene.render(M, W, H, f)
+        assert samples == osamples
+        assert psnr(rgb, orgb) >= PSNR_MIN
+        assert np.abs(dep - odep).max() <= DEPTH_TOL
+
+
+def test_tc_and_fp32_agree(r32, rtc, cuda, nes_lib):
+    M = nes_lib.shell_poses(6, 1, 1.2, 2.0)[0]
+    W, H = 160, 120
+    f = nes_lib.focal_from_fov(W, 100.0)
+    (a, da), = render_gpu(r32, cuda, [(M, W, H, f)])
+    (b, db), = render_gpu(rtc, cuda, [(M, W, H, f)])
+    assert psnr(a, b) >= PSNR_MIN
+    assert np.abs(da - db).max() <= DEPTH_TOL
+    assert rtc.last_sample_count() == r32.last_sample_count()
 
 
 def test_occupancy_matches_oracle(r32, scene0):
