@@ -1,25 +1,36 @@
 // march_tc.cu -- FP16 tensor-core march: the renderer's density and colour
 // MLPs (the external instant-ngp-renderer neserver calls over TCP,
-// src/server.cpp:161-194) evaluated with tcgen05 MMAs.
+// src/server.cpp:161-194) evaluated with tcgen05 MMAs whose activations never
+// leave tensor memory, overlapped with the hash-grid gathers by warp
+// specialisation.
 //
-// Structure (one persistent CTA of 128 threads, up to 4 CTAs per SM):
-//  - each thread owns one ray slot; per iteration every active slot
-//    contributes its next occupied sample, so one iteration is one
-//    128-sample tile (M = 128);
-//  - the thread encodes its sample from the FP16 hash table (FP32
-//    interpolation) and writes the 32 features as one FP16 row of the A tile
-//    in shared memory (K-major canonical layout, no swizzle);
-//  - one elected thread issues the five layers as tcgen05.mma kind::f16
-//    (32->64, 64->16, 32->64, 64->64, 64->16 [3 used]) with FP32
-//    accumulators in TMEM (128 columns per CTA); after each layer every
-//    thread loads its own TMEM lane (= its sample), applies ReLU / exp /
-//    sigmoid in FP32 and writes the next FP16 operand row;
-//  - the weights (FP16, already in operand layout, 20 KiB) are staged once
-//    per CTA with one bulk TMA copy;
-//  - transmittance, compositing and depth stay in FP32 per thread.
-// TMEM safety: 128 columns x at most 4 resident CTAs = 512 columns per SM;
-// the dynamic shared-memory request (50 KiB) makes a fifth CTA impossible,
-// so tcgen05.alloc never waits on a CTA that will not exit.
+// Why this shape: the march is bound by the ~128 scattered 4-byte table
+// gathers per sample, and their speed depends on the L1 cache; with more than
+// ~64 KiB of shared memory per SM the L1 shrinks below the coarse levels'
+// working set and the gathers run ~2.5x slower.  So shared memory holds only
+// the MLP weights (the B operands, 20 KiB) and small per-row hand-off arrays;
+// every A operand (encoded features, hidden layers, colour input) lives in
+// TMEM and feeds tcgen05.mma directly.
+//
+// One CTA per SM: 4 groups x (4 ENCODER warps + 4 MLP warps) = 1024 threads.
+//  - ENCODER thread = one ray slot.  Per tile it claims rays (a warp-wide
+//    chunk of 32 at a time), encodes its slot's next occupied sample from the
+//    FP16 table (FP32 interpolation), writes the 32 FP16 features as its
+//    TMEM lane of the tile (16 columns) and marks the tile full.  Encoders run
+//    one tile ahead of the MLP (two tile buffers), then composite the
+//    previous tile's results (FP32 transmittance, colour, depth).
+//  - MLP thread = TMEM lane = tile row.  One thread issues each layer
+//    (32->64, 64->16, 32->64, 64->64, 64->16 [3 used]) as tcgen05.mma
+//    kind::f16 with A from TMEM and B from shared memory, FP32 accumulators in
+//    TMEM; between layers every thread loads its lane, applies ReLU / exp and
+//    stores the next FP16 A operand back to TMEM.
+//  - A sample encoded speculatively for a ray that terminates early
+//    (T < 1e-4) is discarded at compositing time.
+// TMEM (512 columns): group g encoder tiles at 32g (+16 for the second
+// buffer), MLP hidden activations at 128+96g (32 columns of packed FP16),
+// accumulator after them (64 FP32 columns).  Two CTAs cannot share an SM:
+// 1024 threads x >32 registers fill the register file, and the launcher
+// checks it.
 #include <cuda_fp16.h>
 
 #include "kernels.h"
@@ -29,8 +40,15 @@ namespace nes {
 
 namespace {
 
-constexpr int kTcThreads = 128;
-constexpr uint32_t kTmemCols = 128;
+constexpr int kGroups = 4;
+constexpr int kRoleThreads = 128;  // encoder threads = MLP threads = tile rows
+constexpr int kGroupThreads = 2 * kRoleThreads;
+constexpr int kTcThreads = kGroups * kGroupThreads;  // 1024
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kEncColsPerGroup = 32;  // two 16-column tile buffers
+constexpr uint32_t kMlpBase = kGroups * kEncColsPerGroup;
+constexpr uint32_t kMlpColsPerGroup = 96;  // 64 accumulator + 32 hidden activations
+static_assert(kMlpBase + kGroups * kMlpColsPerGroup <= kTmemCols, "TMEM column budget");
 
 // Weight image (bytes) in operand layout: [N][K] K-major, core matrices 8x16B.
 constexpr int kWoffDW1 = 0;      // N=64, K=32
@@ -40,133 +58,145 @@ constexpr int kWoffCW2 = 10240;  // N=64, K=64
 constexpr int kWoffCW3 = 18432;  // N=16 (rows 3..15 zero), K=64
 constexpr int kWBytes = 20480;
 
-// Shared-memory map (bytes from a 1024-aligned base).
-constexpr int kOffW = 0;
-constexpr int kOffA = kOffW + kWBytes;  // 128 x 32 FP16 = 8 KiB
-constexpr int kOffH = kOffA + 8192;     // 128 x 64 FP16 = 16 KiB
-constexpr int kOffBar = kOffH + 16384;  // two mbarriers
-constexpr int kOffSlot = kOffBar + 16;  // TMEM address
-constexpr int kSmemUsed = kOffSlot + 16;
-constexpr int kSmemRequest = 50 * 1024 + 1024;  // 5 x (this + 1 KiB reserved) > 228 KiB per SM
-static_assert(kSmemUsed + 1024 <= kSmemRequest, "shared memory map exceeds the request");
-static_assert(5 * (kSmemRequest + 1024) > 228 * 1024, "a fifth CTA per SM would fit: TMEM oversubscribed");
+// Per-group shared memory: per-row ray directions and results for both tile
+// buffers, stop flags and mbarriers.
+constexpr int kGOffDir = 0;                         // [2][128] float4 (d, unused)
+constexpr int kGOffRes = kGOffDir + 2 * 128 * 16;   // [2][128] float4 (sigma, r, g, b)
+constexpr int kGOffStop = kGOffRes + 2 * 128 * 16;  // [2] uint32
+constexpr int kGOffBar = kGOffStop + 16;            // full0, full1, done0, done1, mma
+constexpr int kGroupBytes = (kGOffBar + 5 * 8 + 127) / 128 * 128;
 
-// Byte offset of 16-byte chunk c (K elements 8c..8c+7) of row m in a
-// K-major operand with K columns: core matrices 8 rows x 16 B, K-chunks
-// adjacent (LBO = 128 B), 8-row groups K*16 B apart (SBO).
-__host__ __device__ constexpr int op_chunk(int m, int c, int K) { return (m >> 3) * (K * 16) + c * 128 + (m & 7) * 16; }
+constexpr int kOffW = 0;
+constexpr int kOffGroups = kOffW + kWBytes;
+constexpr int kOffBarW = kOffGroups + kGroups * kGroupBytes;
+constexpr int kOffSlot = kOffBarW + 8;
+constexpr int kSmemUsed = kOffSlot + 8;
+constexpr int kSmemRequest = kSmemUsed + 1024;  // slack to align the base to 1 KiB
+// Keep the shared-memory carve-out at the 64 KiB configuration (L1 >= 192 KiB).
+static_assert(kSmemRequest + 1024 <= 64 * 1024, "shared memory above the L1-friendly carve-out");
+
+// Byte offset of 16-byte chunk c (K elements 8c..8c+7) of row n in a
+// K-major shared-memory operand with K columns (core matrices 8 rows x 16 B,
+// K-chunks adjacent: LBO = 128 B, 8-row groups K*16 B apart: SBO).
+__host__ __device__ constexpr int op_chunk(int n, int c, int K) { return (n >> 3) * (K * 16) + c * 128 + (n & 7) * 16; }
 
 __device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+__device__ __forceinline__ uint32_t pk(float a, float b) { return h2u(__floats2half2_rn(a, b)); }
+__device__ __forceinline__ uint32_t pk_relu(float a, float b) { return pk(fmaxf(a, 0.0f), fmaxf(b, 0.0f)); }
 
-__device__ __forceinline__ void store_row_chunks(uint8_t* tile, int row, int K, int c0, const uint32_t* w, int nchunks) {
+// Level L of the FP16 table at x -> its two features packed as FP16 (FP32 interpolation).
+template <int L>
+__device__ __forceinline__ uint32_t encode_level(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
+                                                 const float3& x) {
+  constexpr int N = level_res(L);
+  const LevelCell c = level_cell(x, N);
+  uint32_t idx[8];
+  corner_indices(c, N, (dense_mask >> L) & 1u, T, idx);
+  float w[8];
+  corner_weights(c, w);
+  const __half2* tab = table + (size_t)L * T;
+  float a0 = 0.0f, a1 = 0.0f;
 #pragma unroll
-  for (int q = 0; q < nchunks; ++q)
-    *reinterpret_cast<uint4*>(tile + op_chunk(row, c0 + q, K)) = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+  for (int k = 0; k < 8; ++k) {
+    const float2 e = __half22float2(__ldg(tab + idx[k]));
+    a0 = fmaf(w[k], e.x, a0);
+    a1 = fmaf(w[k], e.y, a1);
+  }
+  return pk(a0, a1);
 }
 
-// 32 FP32 TMEM columns -> ReLU -> FP16 -> 4 chunks of an H row (K = 64).
-__device__ __forceinline__ void relu_to_h(uint32_t taddr, uint8_t* H, int row, int c0) {
-  float v[32];
-  tc::tmem_ld32(taddr, v);
-  uint32_t w[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) w[k] = h2u(__floats2half2_rn(fmaxf(v[2 * k], 0.0f), fmaxf(v[2 * k + 1], 0.0f)));
-  store_row_chunks(H, row, 64, c0, w, 4);
+// Four levels -> TMEM columns 4C..4C+3 of this lane (no wait).  The store is
+// warp-collective, so every lane executes it; lanes without a sample store
+// zeros.
+template <int C>
+__device__ __forceinline__ void encode_chunk(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
+                                             const float3& x, bool has, uint32_t taddr) {
+  uint32_t a = 0u, b = 0u, c = 0u, d = 0u;
+  if (has) {
+    a = encode_level<4 * C + 0>(table, T, dense_mask, x);
+    b = encode_level<4 * C + 1>(table, T, dense_mask, x);
+    c = encode_level<4 * C + 2>(table, T, dense_mask, x);
+    d = encode_level<4 * C + 3>(table, T, dense_mask, x);
+  }
+  tc::tmem_st4(taddr + 4 * C, a, b, c, d);
 }
 
-// FP16 table, FP32 interpolation.
-__device__ __forceinline__ void encode_fp16(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
-                                            const float3& x, float feat[kEnc]) {
+// D[128 x N] = A[128 x K] (TMEM) * B[N x K]^T (shared), K in steps of 16
+// (8 TMEM columns of packed FP16 per step).
+__device__ __forceinline__ void mma_layer(uint32_t d_tmem, uint32_t a_tmem, uint32_t b, int K, uint32_t idesc) {
+  for (int j = 0; j < K / 16; ++j)
+    tc::mma_f16_at(d_tmem, a_tmem + j * 8, tc::sdesc(b + j * 256, 128, K * 16), idesc, j > 0 ? 1u : 0u);
+}
+
+// 64 accumulator columns -> ReLU -> FP16 -> 32 hidden-activation columns.
+__device__ __forceinline__ void relu_to_h(uint32_t d_row, uint32_t h_row) {
 #pragma unroll
-  for (int l = 0; l < kLevels; ++l) {
-    const int N = level_res(l);
-    const LevelCell c = level_cell(x, N);
-    uint32_t idx[8];
-    corner_indices(c, N, (dense_mask >> l) & 1u, T, idx);
-    float w[8];
-    corner_weights(c, w);
-    const __half2* tab = table + (size_t)l * T;
-    float a0 = 0.0f, a1 = 0.0f;
+  for (int half = 0; half < 2; ++half) {
+    float v[32];
+    tc::tmem_ld32(d_row + 32 * half, v);
+    uint32_t w[16];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const float2 e = __half22float2(__ldg(tab + idx[k]));
-      a0 = fmaf(w[k], e.x, a0);
-      a1 = fmaf(w[k], e.y, a1);
-    }
-    feat[2 * l] = a0;
-    feat[2 * l + 1] = a1;
+    for (int k = 0; k < 16; ++k) w[k] = pk_relu(v[2 * k], v[2 * k + 1]);
+    tc::tmem_st16(h_row + 16 * half, w);
   }
 }
 
-// Issues one layer: D[128 x N] = A[128 x K] * B[N x K]^T, K in steps of 16.
-__device__ __forceinline__ void mma_layer(uint32_t d_tmem, uint32_t a, int a_K, uint32_t b, int b_K, int K,
-                                          uint32_t idesc) {
-  for (int j = 0; j < K / 16; ++j)
-    tc::mma_f16(d_tmem, tc::sdesc(a + j * 256, 128, a_K * 16), tc::sdesc(b + j * 256, 128, b_K * 16), idesc,
-                j > 0 ? 1u : 0u);
+__device__ __forceinline__ void write_ray(const ViewBatch& vb, const DevScratch& s, uint32_t id, float cr, float cg,
+                                          float cb, float dep) {
+  const RayMeta m = s.ray_meta[id];
+  const DevView& V = vb.v[m.view];
+  if (V.rgb) {
+    V.rgb[(size_t)m.pixel * 3 + 0] = cr;
+    V.rgb[(size_t)m.pixel * 3 + 1] = cg;
+    V.rgb[(size_t)m.pixel * 3 + 2] = cb;
+  }
+  if (V.depth) V.depth[m.pixel] = dep;
 }
 
-struct RaySlot {
-  bool active = false;
-  int view = 0, pixel = 0, n = 0, i = 0;
+// Encoder-side state of one ray slot.  Two compositing contexts: the ray
+// being encoded and, for one tile after a ray switch, the previous ray.
+struct Slot {
+  bool enc_live = false;
+  int ec = 1;  // context of the ray being encoded (the first ray gets 0)
   float3 o, d;
-  float ts = 0.0f, T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f, dep = 0.0f;
-  uint32_t sh[8];  // SH16(d) as FP16 pairs
+  float ts = 0.0f;
+  int n = 0, ei = 0;
+  uint32_t id0 = 0, id1 = 0;
+  float T0 = 1.0f, r0 = 0.0f, g0 = 0.0f, b0 = 0.0f, z0 = 0.0f;
+  float T1 = 1.0f, r1 = 0.0f, g1 = 0.0f, b1 = 0.0f, z1 = 0.0f;
+  uint32_t live = 0;      // bit c: context c still accumulating
+  uint32_t tag0 = 0, tag1 = 0;  // per buffer: bit0 sample, bit1 context, bit2 last sample of its ray
+  float t0 = 0.0f, t1 = 0.0f;
 };
 
-__device__ __forceinline__ void write_ray(const ViewBatch& vb, const RaySlot& r) {
-  const DevView& V = vb.v[r.view];
-  if (V.rgb) {
-    V.rgb[(size_t)r.pixel * 3 + 0] = r.cr;
-    V.rgb[(size_t)r.pixel * 3 + 1] = r.cg;
-    V.rgb[(size_t)r.pixel * 3 + 2] = r.cb;
-  }
-  if (V.depth) V.depth[r.pixel] = r.dep;
+__device__ __forceinline__ void skip_empty(const DevScene& sc, Slot& q) {
+  while (q.ei < q.n && !occupied(sc.occ, sample_pos(q.o, q.d, fmaf((float)q.ei + 0.5f, kDt, q.ts)))) ++q.ei;
 }
 
-// Advances r.i to the next occupied sample (or r.n).
-__device__ __forceinline__ void skip_empty(const DevScene& sc, RaySlot& r) {
-  while (r.i < r.n && !occupied(sc.occ, sample_pos(r.o, r.d, fmaf((float)r.i + 0.5f, kDt, r.ts)))) ++r.i;
-}
-
-__device__ __forceinline__ void start_ray(const ViewBatch& vb, const DevScene& sc, const DevScratch& s, uint32_t id,
-                                          RaySlot& r) {
-  const float4 rd = s.ray_dt[id];
-  const RayMeta m = s.ray_meta[id];
-  r.view = m.view;
-  r.pixel = m.pixel;
-  r.n = m.n;
-  r.i = 0;
-  r.ts = rd.w;
-  r.d = make_float3(rd.x, rd.y, rd.z);
-  const DevView& V = vb.v[m.view];
-  r.o = make_float3(V.M[3], V.M[7], V.M[11]);
-  r.T = 1.0f;
-  r.cr = r.cg = r.cb = r.dep = 0.0f;
-  float sh[16];
-  sh16(r.d, sh);
-#pragma unroll
-  for (int k = 0; k < 8; ++k) r.sh[k] = h2u(__floats2half2_rn(sh[2 * k], sh[2 * k + 1]));
-  skip_empty(sc, r);
-  r.active = r.i < r.n;
-  if (!r.active) write_ray(vb, r);
-}
-
-__global__ void __launch_bounds__(kTcThreads, 4)
+__global__ void __launch_bounds__(kTcThreads, 1)
 march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  // Align the working base to 1024 B (the request leaves room for it).
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  uint64_t* bar_w = reinterpret_cast<uint64_t*>(smem + kOffBar);
-  uint64_t* bar_mma = bar_w + 1;
+  const int g = tid / kGroupThreads;
+  const bool is_mlp = (tid % kGroupThreads) >= kRoleThreads;
+  const int row = tid % kRoleThreads;  // tile row = TMEM lane
+  uint8_t* G = smem + kOffGroups + g * kGroupBytes;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(G + kGOffBar);  // full0, full1, done0, done1, mma
+  uint32_t* stop = reinterpret_cast<uint32_t*>(G + kGOffStop);
+  float4* dirs = reinterpret_cast<float4*>(G + kGOffDir);
+  float4* res = reinterpret_cast<float4*>(G + kGOffRes);
+  uint64_t* bar_w = reinterpret_cast<uint64_t*>(smem + kOffBarW);
   uint32_t* slot = reinterpret_cast<uint32_t*>(smem + kOffSlot);
-  uint8_t* A = smem + kOffA;
-  uint8_t* Hs = smem + kOffH;
+  const uint32_t enc_bar = 1 + 2 * g, mlp_bar = 2 + 2 * g;
 
   if (tid == 0) {
     tc::mbar_init(bar_w, 1);
-    tc::mbar_init(bar_mma, 1);
+    for (int k = 0; k < kGroups; ++k) {
+      uint64_t* b = reinterpret_cast<uint64_t*>(smem + kOffGroups + k * kGroupBytes + kGOffBar);
+      for (int j = 0; j < 4; ++j) tc::mbar_init(b + j, kRoleThreads);
+      tc::mbar_init(b + 4, 1);
+    }
     tc::fence_mbar_init();
   }
   if (warp == 0) {
@@ -177,179 +207,224 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = *slot;
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;  // this warp's TMEM lane quarter
+  const uint32_t enc_cols = tmem + g * kEncColsPerGroup;        // + 16 * buffer
+  bool fail = false;
   if (tid == 0) {
     tc::mbar_arrive_expect_tx(bar_w, kWBytes);
     tc::bulk_g2s(smem + kOffW, sc.tc_weights, kWBytes, bar_w);
+    fail = !tc::mbar_wait(bar_w, 0);
   }
-  bool fail = !tc::mbar_wait(bar_w, 0);
-  uint32_t phase = 0;
+  fail = __syncthreads_or(fail);
 
-  const uint32_t sW = tc::smem_addr(smem + kOffW), sA = tc::smem_addr(A), sH = tc::smem_addr(Hs);
-  const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lane quarter
-  constexpr uint32_t id64 = tc::idesc_f16_f32(128, 64), id16 = tc::idesc_f16_f32(128, 16);
-  const uint32_t nrays = min(s.counters[kCtrRays], s.max_rays);
-
-  RaySlot r;
-  uint32_t chunk_next = 0, chunk_end = 0;
-  bool exhausted = false;
   unsigned long long my_samples = 0;
+  if (!fail && is_mlp) {
+    // ======================= MLP warps =======================
+    const uint32_t sW = tc::smem_addr(smem + kOffW);
+    const uint32_t h_col = tmem + kMlpBase + g * kMlpColsPerGroup;  // hidden activations (lane 0)
+    const uint32_t d_col = h_col + 32;                              // accumulator (lane 0)
+    const uint32_t d_row = d_col + lane_off, h_row = h_col + lane_off;
+    constexpr uint32_t id64 = tc::idesc_f16_f32(128, 64), id16 = tc::idesc_f16_f32(128, 16);
+    uint32_t pf0 = 0, pf1 = 0, pm = 0;
 
-  for (;;) {
-    // Refill idle slots from a per-warp chunk of 32 ray ids (one atomic per
-    // 32 rays).  Warp-uniform loop.
+    // One layer: publish this thread's TMEM writes, one thread issues and
+    // waits, the warps learn the outcome.
+    auto layer = [&](uint32_t a_tmem, uint32_t b_off, int K, uint32_t idesc, bool publish) -> bool {
+      if (publish) {
+        tc::fence_before();
+        tc::named_sync(mlp_bar, kRoleThreads);
+      }
+      bool bad = false;
+      if (row == 0) {
+        tc::fence_after();
+        mma_layer(d_col, a_tmem, sW + b_off, K, idesc);
+        tc::mma_commit(bar + 4);
+        bad = !tc::mbar_wait(bar + 4, pm);
+      }
+      pm ^= 1u;
+      bad = tc::named_sync_or(mlp_bar, kRoleThreads, bad);
+      tc::fence_after();
+      return !bad;
+    };
+
+    auto run_tile = [&](int b, uint32_t& pf) -> int {  // 1 processed, 0 stop, -1 failure
+      bool bad = false, st = false;
+      if (row == 0) {
+        bad = !tc::mbar_wait_sleep(bar + b, pf);
+        st = bad || stop[b] != 0;
+      }
+      pf ^= 1u;
+      if (tc::named_sync_or(mlp_bar, kRoleThreads, bad)) return -1;
+      if (tc::named_sync_or(mlp_bar, kRoleThreads, st)) return 0;
+      const uint32_t a_col = enc_cols + 16 * b;  // encoded features, later the colour input
+      // density 32 -> 64 -> 16
+      if (!layer(a_col, kWoffDW1, 32, id64, false)) return -1;
+      relu_to_h(d_row, h_row);
+      if (!layer(h_col, kWoffDW2, 64, id16, true)) return -1;
+      float sigma;
+      {
+        float v[16];
+        tc::tmem_ld16(d_row, v);
+        sigma = expf(v[0] - 1.0f);
+        const float4 dd = dirs[b * 128 + row];
+        float sh[16];
+        sh16(make_float3(dd.x, dd.y, dd.z), sh);
+        uint32_t w[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) w[k] = pk(sh[2 * k], sh[2 * k + 1]);
+#pragma unroll
+        for (int k = 0; k < 7; ++k) w[8 + k] = pk(v[1 + 2 * k], v[2 + 2 * k]);
+        w[15] = pk(v[15], 0.0f);
+        tc::tmem_st16(a_col + lane_off, w);  // layer 1 is done with this buffer
+      }
+      // colour 32 -> 64 -> 64 -> 3
+      if (!layer(a_col, kWoffCW1, 32, id64, true)) return -1;
+      relu_to_h(d_row, h_row);
+      if (!layer(h_col, kWoffCW2, 64, id64, true)) return -1;
+      relu_to_h(d_row, h_row);
+      if (!layer(h_col, kWoffCW3, 64, id16, true)) return -1;
+      float v5[16];
+      tc::tmem_ld16(d_row, v5);
+      tc::fence_before();
+      res[b * 128 + row] = make_float4(sigma, sigmoidf(v5[0]), sigmoidf(v5[1]), sigmoidf(v5[2]));
+      tc::mbar_arrive(bar + 2 + b);
+      return 1;
+    };
+
     for (;;) {
-      const unsigned need = __ballot_sync(0xffffffffu, !r.active);
-      if (need == 0 || exhausted) break;
-      const uint32_t avail = chunk_end - chunk_next;
-      const uint32_t rank = (uint32_t)__popc(need & ((1u << lane) - 1u));
-      if (!r.active && rank < avail) start_ray(vb, sc, s, chunk_next + rank, r);
-      const uint32_t cnt = (uint32_t)__popc(need);
-      if (cnt <= avail) {
-        chunk_next += cnt;
-      } else {
-        uint32_t b = 0;
-        if (lane == 0) b = atomicAdd(s.counters + kCtrCursor, 32u);
-        b = __shfl_sync(0xffffffffu, b, 0);
-        if (b >= nrays) {
-          exhausted = true;
+      int rc = run_tile(0, pf0);
+      if (rc <= 0) { fail = rc < 0; break; }
+      rc = run_tile(1, pf1);
+      if (rc <= 0) { fail = rc < 0; break; }
+    }
+  } else if (!fail) {
+    // ======================= encoder warps =======================
+    const uint32_t nrays = min(s.counters[kCtrRays], s.max_rays);
+    Slot q;
+    uint32_t chunk_next = 0, chunk_end = 0, pd0 = 0, pd1 = 0;
+    bool exhausted = false;
+
+    // Encodes the slot's next sample into buffer b and marks it full.
+    // Returns whether any slot of the group had a sample.
+    auto encode_step = [&](int b) -> bool {
+      for (;;) {  // refill (warp-uniform)
+        const unsigned need = __ballot_sync(0xffffffffu, !q.enc_live);
+        if (need == 0 || exhausted) break;
+        const uint32_t avail = chunk_end - chunk_next;
+        const uint32_t rank = (uint32_t)__popc(need & ((1u << lane) - 1u));
+        if (!q.enc_live && rank < avail) {
+          const uint32_t id = chunk_next + rank;
+          const float4 rd = s.ray_dt[id];
+          const RayMeta m = s.ray_meta[id];
+          const DevView& V = vb.v[m.view];
+          q.o = make_float3(V.M[3], V.M[7], V.M[11]);
+          q.d = make_float3(rd.x, rd.y, rd.z);
+          q.ts = rd.w;
+          q.n = m.n;
+          q.ei = 0;
+          skip_empty(sc, q);
+          if (q.ei < q.n) {
+            q.enc_live = true;
+            q.ec ^= 1;
+            if (q.ec == 0) {
+              q.id0 = id; q.T0 = 1.0f; q.r0 = q.g0 = q.b0 = q.z0 = 0.0f;
+            } else {
+              q.id1 = id; q.T1 = 1.0f; q.r1 = q.g1 = q.b1 = q.z1 = 0.0f;
+            }
+            q.live |= 1u << q.ec;
+          } else {
+            write_ray(vb, s, id, 0.0f, 0.0f, 0.0f, 0.0f);  // no occupied sample
+          }
+        }
+        const uint32_t cnt = (uint32_t)__popc(need);
+        if (cnt <= avail) {
+          chunk_next += cnt;
         } else {
-          chunk_next = b;
-          chunk_end = min(b + 32u, nrays);
+          uint32_t base = 0;
+          if (lane == 0) base = atomicAdd(s.counters + kCtrCursor, 32u);
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (base >= nrays) {
+            exhausted = true;
+          } else {
+            chunk_next = base;
+            chunk_end = min(base + 32u, nrays);
+          }
         }
       }
-    }
-    const bool has = r.active;
-    if (!__syncthreads_or(has)) break;  // every slot idle and every warp's queue empty
-
-    // ---- encode this slot's sample into row `tid` of A (K = 32) ----
-    float t = 0.0f;
-    {
-      uint32_t w[16];
+      const uint32_t a_row = enc_cols + 16 * b + lane_off;
+      const bool has = q.enc_live;
+      uint32_t tag = 0;
+      const float t = has ? fmaf((float)q.ei + 0.5f, kDt, q.ts) : 0.0f;
+      const float3 x = sample_pos(q.o, q.d, t);
+      encode_chunk<0>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
+      encode_chunk<1>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
+      encode_chunk<2>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
+      encode_chunk<3>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
       if (has) {
-        t = fmaf((float)r.i + 0.5f, kDt, r.ts);
-        float feat[kEnc];
-        encode_fp16(sc.table16, sc.T, sc.dense_mask, sample_pos(r.o, r.d, t), feat);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) w[k] = h2u(__floats2half2_rn(feat[2 * k], feat[2 * k + 1]));
+        dirs[b * 128 + row] = make_float4(q.d.x, q.d.y, q.d.z, 0.0f);
+        tag = 1u | ((uint32_t)q.ec << 1);
+        ++q.ei;
+        skip_empty(sc, q);
+        if (q.ei >= q.n) {
+          tag |= 4u;
+          q.enc_live = false;
+        }
       } else {
-#pragma unroll
-        for (int k = 0; k < 16; ++k) w[k] = 0u;
+        dirs[b * 128 + row] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
       }
-      store_row_chunks(A, tid, 32, 0, w, 4);
-    }
+      if (b == 0) { q.tag0 = tag; q.t0 = t; } else { q.tag1 = tag; q.t1 = t; }
+      tc::tmem_wait_st();
+      tc::fence_before();
+      const bool any = tc::named_sync_or(enc_bar, kRoleThreads, has);
+      if (row == 0) stop[b] = any ? 0u : 1u;
+      tc::mbar_arrive(bar + b);
+      return any;
+    };
 
-    // ---- layer 1: density 32 -> 64, D at TMEM columns 0..63 ----
-    tc::fence_async_smem();
-    tc::fence_before();
-    if (__syncthreads_or(fail)) break;
-    if (tid == 0) {
-      tc::fence_after();
-      mma_layer(tmem + 0, sA, 32, sW + kWoffDW1, 32, 32, id64);
-      tc::mma_commit(bar_mma);
-    }
-    fail |= !tc::mbar_wait(bar_mma, phase);
-    phase ^= 1u;
-    tc::fence_after();
-    relu_to_h(t_row + 0, Hs, tid, 0);
-    relu_to_h(t_row + 32, Hs, tid, 4);
-
-    // ---- layer 2: density 64 -> 16, D at columns 64..79 ----
-    tc::fence_async_smem();
-    tc::fence_before();
-    if (__syncthreads_or(fail)) break;
-    if (tid == 0) {
-      tc::fence_after();
-      mma_layer(tmem + 64, sH, 64, sW + kWoffDW2, 64, 64, id16);
-      tc::mma_commit(bar_mma);
-    }
-    fail |= !tc::mbar_wait(bar_mma, phase);
-    phase ^= 1u;
-    tc::fence_after();
-    float sigma;
-    {
-      float v[16];
-      tc::tmem_ld16(t_row + 64, v);
-      sigma = expf(v[0] - 1.0f);
-      uint32_t w[16];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) w[k] = r.sh[k];
-#pragma unroll
-      for (int k = 0; k < 7; ++k) w[8 + k] = h2u(__floats2half2_rn(v[1 + 2 * k], v[2 + 2 * k]));
-      w[15] = h2u(__floats2half2_rn(v[15], 0.0f));
-      store_row_chunks(A, tid, 32, 0, w, 4);
-    }
-
-    // ---- layer 3: colour 32 -> 64, D at columns 0..63 ----
-    tc::fence_async_smem();
-    tc::fence_before();
-    if (__syncthreads_or(fail)) break;
-    if (tid == 0) {
-      tc::fence_after();
-      mma_layer(tmem + 0, sA, 32, sW + kWoffCW1, 32, 32, id64);
-      tc::mma_commit(bar_mma);
-    }
-    fail |= !tc::mbar_wait(bar_mma, phase);
-    phase ^= 1u;
-    tc::fence_after();
-    relu_to_h(t_row + 0, Hs, tid, 0);
-    relu_to_h(t_row + 32, Hs, tid, 4);
-
-    // ---- layer 4: colour 64 -> 64, D at columns 64..127 ----
-    tc::fence_async_smem();
-    tc::fence_before();
-    if (__syncthreads_or(fail)) break;
-    if (tid == 0) {
-      tc::fence_after();
-      mma_layer(tmem + 64, sH, 64, sW + kWoffCW2, 64, 64, id64);
-      tc::mma_commit(bar_mma);
-    }
-    fail |= !tc::mbar_wait(bar_mma, phase);
-    phase ^= 1u;
-    tc::fence_after();
-    relu_to_h(t_row + 64, Hs, tid, 0);
-    relu_to_h(t_row + 96, Hs, tid, 4);
-
-    // ---- layer 5: colour 64 -> 3 (N = 16), D at columns 0..15 ----
-    tc::fence_async_smem();
-    tc::fence_before();
-    if (__syncthreads_or(fail)) break;
-    if (tid == 0) {
-      tc::fence_after();
-      mma_layer(tmem + 0, sH, 64, sW + kWoffCW3, 64, 64, id16);
-      tc::mma_commit(bar_mma);
-    }
-    fail |= !tc::mbar_wait(bar_mma, phase);
-    phase ^= 1u;
-    tc::fence_after();
-    float v5[16];
-    tc::tmem_ld16(t_row + 0, v5);
-    tc::fence_before();
-
-    // ---- composite in FP32 ----
-    if (has) {
+    // Waits for buffer b's results and composites them.  False on timeout.
+    auto composite_step = [&](int b, uint32_t& pd) -> bool {
+      bool bad = false;
+      if (row == 0) bad = !tc::mbar_wait_sleep(bar + 2 + b, pd);
+      pd ^= 1u;
+      if (tc::named_sync_or(enc_bar, kRoleThreads, bad)) return false;
+      const uint32_t tag = b == 0 ? q.tag0 : q.tag1;
+      if (!(tag & 1u)) return true;
+      const int c = (tag >> 1) & 1;
+      if (!((q.live >> c) & 1u)) return true;  // ray already finished: discard the speculative sample
+      const float4 v = res[b * 128 + row];
+      const float t = b == 0 ? q.t0 : q.t1;
       ++my_samples;
-      const float alpha = -expm1f(-sigma * kDt);
-      const float wgt = r.T * alpha;
-      r.cr = fmaf(wgt, sigmoidf(v5[0]), r.cr);
-      r.cg = fmaf(wgt, sigmoidf(v5[1]), r.cg);
-      r.cb = fmaf(wgt, sigmoidf(v5[2]), r.cb);
-      r.dep = fmaf(wgt, t, r.dep);
-      r.T -= wgt;
-      ++r.i;
-      if (r.T >= kTStop) skip_empty(sc, r);
-      if (r.T < kTStop || r.i >= r.n) {
-        write_ray(vb, r);
-        r.active = false;
+      const float alpha = -expm1f(-v.x * kDt);
+      float& T = c == 0 ? q.T0 : q.T1;
+      float& cr = c == 0 ? q.r0 : q.r1;
+      float& cg = c == 0 ? q.g0 : q.g1;
+      float& cb = c == 0 ? q.b0 : q.b1;
+      float& z = c == 0 ? q.z0 : q.z1;
+      const float wgt = T * alpha;
+      cr = fmaf(wgt, v.y, cr);
+      cg = fmaf(wgt, v.z, cg);
+      cb = fmaf(wgt, v.w, cb);
+      z = fmaf(wgt, t, z);
+      T -= wgt;
+      if (T < kTStop || (tag & 4u)) {
+        write_ray(vb, s, c == 0 ? q.id0 : q.id1, cr, cg, cb, z);
+        q.live &= ~(1u << c);
+        if (c == q.ec) q.enc_live = false;  // early termination: stop encoding this ray
       }
+      return true;
+    };
+
+    bool more = encode_step(0);
+    while (more) {
+      const bool more1 = encode_step(1);
+      if (!composite_step(0, pd0)) { fail = true; break; }
+      if (!more1) break;
+      more = encode_step(0);
+      if (!composite_step(1, pd1)) { fail = true; break; }
     }
   }
 
-  // Teardown: on a failed wait give an outstanding MMA one more bounded wait
-  // before the columns are released; then free TMEM and report.
-  if (fail && tid == 0) {
-    tc::mbar_wait(bar_mma, phase);
-    atomicExch(s.counters + kCtrError, 1u);
-  }
+  if (fail && (tid % kRoleThreads) == 0) atomicExch(s.counters + kCtrError, 1u);
   tc::fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -395,18 +470,23 @@ cudaError_t launch_pack_tc_weights(const float* w32, uint8_t* out, cudaStream_t 
 cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
                             cudaStream_t stream) {
   if (!scene.table16 || !scene.tc_weights) return cudaErrorInvalidValue;
-  static bool attr_set = false;  // idempotent; a race only repeats the call
+  static bool attr_set = false;  // idempotent; a race only repeats the calls
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRequest);
     if (e != cudaSuccess) return e;
+    // Smallest carve-out that holds the request: the rest of the SM's
+    // 256 KiB stays L1 for the hash-table gathers.
+    e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+    if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_tc_kernel, kTcThreads, kSmemRequest);
+  // One CTA per SM is what makes the 512-column TMEM allocation safe: two
+  // 1024-thread CTAs fit on an SM only at <= 32 registers per thread.
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, march_tc_kernel);
   if (e != cudaSuccess) return e;
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  if (per_sm > 4) per_sm = 4;
-  march_tc_kernel<<<num_sms * per_sm, kTcThreads, kSmemRequest, stream>>>(views, scene, s);
+  if (fa.numRegs <= 32) return cudaErrorInvalidConfiguration;
+  march_tc_kernel<<<num_sms, kTcThreads, kSmemRequest, stream>>>(views, scene, s);
   return cudaGetLastError();
 }
 

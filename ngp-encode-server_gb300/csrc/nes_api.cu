@@ -9,7 +9,7 @@
 #include <mutex>
 #include <vector>
 
-#include "../../include/nes_gb300.h"
+#include "nes_gb300.h"
 #include "kernels.h"
 #include "proto.h"
 #include "scene.h"
@@ -75,7 +75,7 @@ int render_batch_locked(nes_ctx* c, const nes_view* views, int n, float* const* 
   ViewBatch vb;
   std::memset(&vb, 0, sizeof(vb));
   vb.n = n;
-  uint64_t total = 0;
+  uint64_t total = 0, threads = 0;
   for (int i = 0; i < n; ++i) {
     if (!view_ok(views[i])) return NES_EINVAL;
     DevView& d = vb.v[i];
@@ -83,13 +83,14 @@ int render_batch_locked(nes_ctx* c, const nes_view* views, int n, float* const* 
     d.W = (int)views[i].width;
     d.H = (int)views[i].height;
     d.focal = views[i].focal_px;
-    d.pix_offset = (uint32_t)total;
+    d.pix_offset = (uint32_t)threads;
     d.rgb = rgb ? rgb[i] : nullptr;
     d.depth = depth ? depth[i] : nullptr;
     total += (uint64_t)views[i].width * views[i].height;
+    threads += view_threads(d.W, d.H);
   }
-  if (total > c->cfg.max_pixels) return NES_EINVAL;
-  vb.total_pixels = (uint32_t)total;
+  if (total > c->cfg.max_pixels || threads > 0xFFFFFFFFull) return NES_EINVAL;
+  vb.total_pixels = (uint32_t)threads;
   NES_CUDA(cudaMemsetAsync(c->scratch.counters, 0, kCtrWords * sizeof(uint32_t), c->stream));
   if (c->profiling) NES_CUDA(cudaEventRecord(c->ev_t[0], c->stream));
   NES_CUDA(launch_raygen(vb, c->scratch, c->stream));

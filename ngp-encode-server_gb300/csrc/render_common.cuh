@@ -18,14 +18,23 @@ struct DevView {
   float M[12];          // 3x4 row-major pose
   int W, H;
   float focal;
-  uint32_t pix_offset;  // first flattened pixel of this view
+  uint32_t pix_offset;  // first ray-generation thread of this view
   float* rgb;           // W*H*3 (may be null)
   float* depth;         // W*H (may be null)
 };
 
+// Ray generation walks each view in 4x8-pixel tiles, one tile per warp, so
+// the 32 rays a warp marches together cover a compact patch (better L1
+// reuse of the hash-table gathers than a 32x1 row strip).
+constexpr int kTileW = 4, kTileH = 8;
+
+__host__ __device__ inline uint32_t view_threads(int W, int H) {
+  return (uint32_t)((W + kTileW - 1) / kTileW) * (uint32_t)((H + kTileH - 1) / kTileH) * (kTileW * kTileH);
+}
+
 struct ViewBatch {
   int n;
-  uint32_t total_pixels;
+  uint32_t total_pixels;  // ray-generation threads (tile-padded pixel count)
   DevView v[kMaxViews];
 };
 

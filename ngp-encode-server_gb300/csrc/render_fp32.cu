@@ -30,16 +30,22 @@ raygen_kernel(const ViewBatch vb, float4* __restrict__ ray_dt, RayMeta* __restri
   float ts = 0.0f;
   if (valid) {
     const DevView& V = vb.v[v];
-    pix = (int)(gid - V.pix_offset);
-    const int px = pix % V.W, py = pix / V.W;
-    n = ray_setup(V.M, V.W, V.H, V.focal, px, py, o, d, ts);
-    if (n == 0) {  // miss: nothing to march, the pixel is black at depth 0
-      if (V.rgb) {
-        V.rgb[(size_t)pix * 3 + 0] = 0.0f;
-        V.rgb[(size_t)pix * 3 + 1] = 0.0f;
-        V.rgb[(size_t)pix * 3 + 2] = 0.0f;
+    const uint32_t local = gid - V.pix_offset;
+    const uint32_t tile = local / (kTileW * kTileH), in = local % (kTileW * kTileH);
+    const uint32_t tiles_x = (uint32_t)(V.W + kTileW - 1) / kTileW;
+    const int px = (int)((tile % tiles_x) * kTileW + in % kTileW);
+    const int py = (int)((tile / tiles_x) * kTileH + in / kTileW);
+    if (px < V.W && py < V.H) {  // tile padding beyond the frame edge does nothing
+      pix = py * V.W + px;
+      n = ray_setup(V.M, V.W, V.H, V.focal, px, py, o, d, ts);
+      if (n == 0) {  // miss: nothing to march, the pixel is black at depth 0
+        if (V.rgb) {
+          V.rgb[(size_t)pix * 3 + 0] = 0.0f;
+          V.rgb[(size_t)pix * 3 + 1] = 0.0f;
+          V.rgb[(size_t)pix * 3 + 2] = 0.0f;
+        }
+        if (V.depth) V.depth[pix] = 0.0f;
       }
-      if (V.depth) V.depth[pix] = 0.0f;
     }
   }
   const unsigned lane = threadIdx.x & 31u;

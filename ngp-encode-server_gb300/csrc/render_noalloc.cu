@@ -28,7 +28,7 @@
 #include <cstring>
 #include <mutex>
 
-#include "../../include/nes_gb300.h"
+#include "nes_gb300.h"
 #include "kernels.h"
 
 namespace nes {
@@ -103,7 +103,7 @@ extern "C" int nes_render_view_noalloc(const float* table_dev, uint32_t log2_tab
   ViewBatch vb;
   std::memset(&vb, 0, sizeof(vb));
   vb.n = 1;
-  vb.total_pixels = (uint32_t)px;
+  vb.total_pixels = view_threads((int)view->width, (int)view->height);
   std::memcpy(vb.v[0].M, view->matrix, sizeof(vb.v[0].M));
   vb.v[0].W = (int)view->width;
   vb.v[0].H = (int)view->height;
