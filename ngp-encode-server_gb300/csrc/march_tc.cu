@@ -44,6 +44,7 @@ constexpr int kGroups = 4;
 constexpr int kRoleThreads = 128;  // encoder threads = MLP threads = tile rows
 constexpr int kGroupThreads = 2 * kRoleThreads;
 constexpr int kTcThreads = kGroups * kGroupThreads;  // 1024
+constexpr uint32_t kLaunchRegs = 64, kEncRegs = 80, kMlpRegs = 48;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kEncColsPerGroup = 32;  // two 16-column tile buffers
 constexpr uint32_t kMlpBase = kGroups * kEncColsPerGroup;
@@ -217,9 +218,16 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
   }
   fail = __syncthreads_or(fail);
 
+  // Registers move from the MLP warpgroups to the gather-bound encoders:
+  // 512 x 80 + 512 x 48 = 1024 x 64, the launch allocation.
+  // Each role sets its budget first thing in its own branch (fail is
+  // CTA-uniform, so a warpgroup either runs its branch whole or not at all).
+  static_assert(kGroups * kRoleThreads * (kEncRegs + kMlpRegs) == kTcThreads * kLaunchRegs, "register split");
+
   unsigned long long my_samples = 0;
   if (!fail && is_mlp) {
     // ======================= MLP warps =======================
+    tc::regs_dec<kMlpRegs>();
     const uint32_t sW = tc::smem_addr(smem + kOffW);
     const uint32_t h_col = tmem + kMlpBase + g * kMlpColsPerGroup;  // hidden activations (lane 0)
     const uint32_t d_col = h_col + 32;                              // accumulator (lane 0)
@@ -239,7 +247,7 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
         tc::fence_after();
         mma_layer(d_col, a_tmem, sW + b_off, K, idesc);
         tc::mma_commit(bar + 4);
-        bad = !tc::mbar_wait(bar + 4, pm);
+        bad = !tc::mbar_wait_sleep(bar + 4, pm);
       }
       pm ^= 1u;
       bad = tc::named_sync_or(mlp_bar, kRoleThreads, bad);
@@ -299,21 +307,30 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
     }
   } else if (!fail) {
     // ======================= encoder warps =======================
+    tc::regs_inc<kEncRegs>();
     const uint32_t nrays = min(s.counters[kCtrRays], s.max_rays);
     Slot q;
-    uint32_t chunk_next = 0, chunk_end = 0, pd0 = 0, pd1 = 0;
+    uint32_t pd0 = 0, pd1 = 0;
     bool exhausted = false;
 
     // Encodes the slot's next sample into buffer b and marks it full.
     // Returns whether any slot of the group had a sample.
     auto encode_step = [&](int b) -> bool {
-      for (;;) {  // refill (warp-uniform)
-        const unsigned need = __ballot_sync(0xffffffffu, !q.enc_live);
-        if (need == 0 || exhausted) break;
-        const uint32_t avail = chunk_end - chunk_next;
-        const uint32_t rank = (uint32_t)__popc(need & ((1u << lane) - 1u));
-        if (!q.enc_live && rank < avail) {
-          const uint32_t id = chunk_next + rank;
+      // Refill a whole warp at once: the warp claims 32 consecutive rays (one
+      // 4x8 pixel tile) only when all its lanes are done, so its 32 samples
+      // stay neighbours in space and each warp-wide gather stays coherent
+      // (lanes refilled one by one drift apart and gather ~2.5x slower).
+      for (;;) {
+        if (__ballot_sync(0xffffffffu, q.enc_live) != 0u || exhausted) break;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(s.counters + kCtrCursor, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= nrays) {
+          exhausted = true;
+          break;
+        }
+        const uint32_t id = base + lane;
+        if (id < nrays) {
           const float4 rd = s.ray_dt[id];
           const RayMeta m = s.ray_meta[id];
           const DevView& V = vb.v[m.view];
@@ -334,20 +351,6 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
             q.live |= 1u << q.ec;
           } else {
             write_ray(vb, s, id, 0.0f, 0.0f, 0.0f, 0.0f);  // no occupied sample
-          }
-        }
-        const uint32_t cnt = (uint32_t)__popc(need);
-        if (cnt <= avail) {
-          chunk_next += cnt;
-        } else {
-          uint32_t base = 0;
-          if (lane == 0) base = atomicAdd(s.counters + kCtrCursor, 32u);
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (base >= nrays) {
-            exhausted = true;
-          } else {
-            chunk_next = base;
-            chunk_end = min(base + 32u, nrays);
           }
         }
       }
