@@ -144,6 +144,77 @@ int nes_render_view_noalloc(const float *table_dev, uint32_t log2_table_size, co
                             const uint32_t *occupancy_dev, const nes_view *view, float *rgb_dev,
                             float *depth_dev, void *stream);
 
+/* ---------------- serving: continuously batched request loop ----------------
+ * Replaces neserver's request loop (src/server.cpp:116-214: one synchronous
+ * FrameRequest in flight per renderer connection, frames handed on through a
+ * bounded FrameQueue/FrameMap with 1 s lock timeouts, src/base/video/
+ * frame_queue.cc:11-39, frame_map.cc:12-53).  Requests are admitted against a
+ * device-memory budget; a scheduler thread flattens the views of all waiting
+ * requests (mono or stereo, any resolution) into one ray queue per batch and
+ * keeps up to max_inflight_batches batches on the GPU, each captured as a
+ * CUDA graph reused per batch shape.  Outputs (YUV420P planes + uint16 depth)
+ * stay in device-resident slots until the caller releases them. */
+
+typedef struct nes_server nes_server;
+
+typedef struct nes_server_config {
+  uint64_t hbm_budget_bytes;     /* batch scratch + outputs of admitted requests */
+  uint32_t max_batch_pixels;     /* pixels per batch (sum over its views) */
+  uint32_t max_inflight_batches; /* batches on the GPU at once (1..4) */
+  uint32_t max_pending;          /* admitted requests waiting for a batch */
+  int32_t use_graphs;            /* 1: CUDA graph per batch shape, 0: plain launches */
+} nes_server_config;
+
+typedef struct nes_request {
+  uint32_t nviews; /* 1 = mono, 2 = stereo (left, right) */
+  nes_view views[2];
+} nes_request;
+
+typedef struct nes_result {
+  uint64_t ticket;
+  int32_t status;  /* NES_OK, or the error of the batch */
+  uint32_t nviews;
+  uint32_t width, height;
+  int32_t linesize[3];        /* YUV420P plane linesizes (32-byte aligned) */
+  uint8_t *y_dev[2], *u_dev[2], *v_dev[2];
+  uint16_t *depth_mm_dev[2];  /* W*H uint16 millimetres per view */
+  double latency_ms;          /* submit -> YUV ready on the device */
+  uint64_t batch_id;
+  uint32_t batch_requests;    /* requests that shared this request's batch */
+  uint32_t batch_views;
+} nes_result;
+
+typedef struct nes_server_stats {
+  uint64_t submitted, rejected, completed, batches;
+  uint64_t pixels, samples;
+  uint64_t graph_instantiations, graph_updates;
+  uint64_t budget_used_bytes;
+} nes_server_stats;
+
+/* Fills cfg with defaults: 8 GiB budget, 2x1920x1832 pixels per batch, two
+ * batches in flight, 256 pending requests, graphs on. */
+void nes_server_config_default(nes_server_config *cfg);
+
+int nes_server_create(nes_ctx *ctx, const nes_server_config *cfg, nes_server **out);
+void nes_server_destroy(nes_server *srv);
+
+/* Admits a request.  NES_EAGAIN when the budget or the pending queue is
+ * full (the request is dropped and counted), NES_EINVAL for a bad request. */
+int nes_submit(nes_server *srv, const nes_request *req, uint64_t *ticket);
+
+/* Waits up to timeout_ns (< 0: forever) for the request; NES_ETIMEDOUT when
+ * it is not finished yet.  The output pointers stay valid until release. */
+int nes_wait(nes_server *srv, uint64_t ticket, int64_t timeout_ns, nes_result *out);
+
+/* Frees a finished request's output slots and its budget share. */
+int nes_release(nes_server *srv, uint64_t ticket);
+
+int nes_server_stats_get(nes_server *srv, nes_server_stats *out);
+
+/* Synchronous device -> host copy of n bytes, e.g. a served YUV plane for the
+ * host H.264 encoder (AVCodecContextManager::send_frame, src/encode.cpp:136). */
+int nes_copy_to_host(void *host_dst, const void *dev_src, size_t n);
+
 /* ---------------- (ii) frame glue ---------------- */
 
 /* RGB24 -> YUV420P, BT.601 studio range, 2x2 chroma average (edge pixels

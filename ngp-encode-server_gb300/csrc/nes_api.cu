@@ -9,43 +9,13 @@
 #include <mutex>
 #include <vector>
 
+#include "ctx_internal.h"
 #include "nes_gb300.h"
 #include "kernels.h"
 #include "proto.h"
 #include "scene.h"
 
 using namespace nes;
-
-struct nes_ctx {
-  nes_config cfg{};
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  std::mutex mu;
-
-  float2* d_table32 = nullptr;
-  __half2* d_table16 = nullptr;
-  float* d_weights = nullptr;
-  uint8_t* d_tc_weights = nullptr;
-  uint32_t* d_occ = nullptr;
-  DevScene scene;
-
-  DevScratch scratch;
-  float* d_rgb = nullptr;        // max_pixels * 3
-  float* d_depth = nullptr;      // max_pixels
-  uint8_t* d_rgb8 = nullptr;     // max_pixels * 3
-  uint8_t* d_gray = nullptr;     // max_pixels
-  uint8_t* d_yuv = nullptr;      // yuv_capacity
-  size_t yuv_capacity = 0;
-  uint16_t* d_depth16 = nullptr; // max_pixels
-
-  uint64_t last_samples = 0;
-  bool samples_pending = false;
-
-  bool profiling = false;
-  bool timings_pending = false;
-  cudaEvent_t ev_t[3] = {nullptr, nullptr, nullptr};
-};
 
 namespace {
 
@@ -71,28 +41,12 @@ bool view_ok(const nes_view& v) {
 
 // Renders views on ctx->stream into the given device outputs.
 int render_batch_locked(nes_ctx* c, const nes_view* views, int n, float* const* rgb, float* const* depth) {
-  if (n < 1 || n > kMaxViews) return NES_EINVAL;
   ViewBatch vb;
-  std::memset(&vb, 0, sizeof(vb));
-  vb.n = n;
-  uint64_t total = 0, threads = 0;
-  for (int i = 0; i < n; ++i) {
-    if (!view_ok(views[i])) return NES_EINVAL;
-    DevView& d = vb.v[i];
-    std::memcpy(d.M, views[i].matrix, sizeof(d.M));
-    d.W = (int)views[i].width;
-    d.H = (int)views[i].height;
-    d.focal = views[i].focal_px;
-    d.pix_offset = (uint32_t)threads;
-    d.rgb = rgb ? rgb[i] : nullptr;
-    d.depth = depth ? depth[i] : nullptr;
-    total += (uint64_t)views[i].width * views[i].height;
-    threads += view_threads(d.W, d.H);
-  }
-  if (total > c->cfg.max_pixels || threads > 0xFFFFFFFFull) return NES_EINVAL;
-  vb.total_pixels = (uint32_t)threads;
-  NES_CUDA(cudaMemsetAsync(c->scratch.counters, 0, kCtrWords * sizeof(uint32_t), c->stream));
+  uint64_t pixels = 0;
+  const int rc = fill_view_batch(views, n, rgb, depth, c->cfg.max_pixels, &vb, &pixels);
+  if (rc != NES_OK) return rc;
   if (c->profiling) NES_CUDA(cudaEventRecord(c->ev_t[0], c->stream));
+  NES_CUDA(cudaMemsetAsync(c->scratch.counters, 0, kCtrWords * sizeof(uint32_t), c->stream));
   NES_CUDA(launch_raygen(vb, c->scratch, c->stream));
   if (c->profiling) NES_CUDA(cudaEventRecord(c->ev_t[1], c->stream));
   if (c->cfg.precision == NES_PREC_FP16_TC)
@@ -510,3 +464,41 @@ int nes_last_timings(nes_ctx* c, float* raygen_ms, float* march_ms) {
 }
 
 }  // extern "C"
+
+namespace nes {
+
+int fill_view_batch(const nes_view* views, int n, float* const* rgb, float* const* depth, uint64_t max_pixels,
+                    ViewBatch* vb, uint64_t* pixels) {
+  if (!views || n < 1 || n > kMaxViews) return NES_EINVAL;
+  std::memset(vb, 0, sizeof(*vb));
+  vb->n = n;
+  uint64_t total = 0, threads = 0;
+  for (int i = 0; i < n; ++i) {
+    if (!view_ok(views[i])) return NES_EINVAL;
+    DevView& d = vb->v[i];
+    std::memcpy(d.M, views[i].matrix, sizeof(d.M));
+    d.W = (int)views[i].width;
+    d.H = (int)views[i].height;
+    d.focal = views[i].focal_px;
+    d.pix_offset = (uint32_t)threads;
+    d.rgb = rgb ? rgb[i] : nullptr;
+    d.depth = depth ? depth[i] : nullptr;
+    total += (uint64_t)views[i].width * views[i].height;
+    threads += view_threads(d.W, d.H);
+  }
+  if (total > max_pixels || threads > 0xFFFFFFFFull) return NES_EINVAL;
+  vb->total_pixels = (uint32_t)threads;
+  *pixels = total;
+  return NES_OK;
+}
+
+cudaError_t enqueue_march(const ViewBatch& vb, const DevScene& scene, const DevScratch& s, int precision, int num_sms,
+                          cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(s.counters, 0, kCtrWords * sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  if ((e = launch_raygen(vb, s, stream)) != cudaSuccess) return e;
+  return precision == NES_PREC_FP16_TC ? launch_march_tc(vb, scene, s, num_sms, stream)
+                                       : launch_march_fp32(vb, scene, s, num_sms, stream);
+}
+
+}  // namespace nes

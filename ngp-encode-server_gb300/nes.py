@@ -63,6 +63,31 @@ class NesFrameRequest(ctypes.Structure):
                 ("matrix", ctypes.c_float * 12)]
 
 
+class NesServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_batch_pixels", ctypes.c_uint32),
+                ("max_inflight_batches", ctypes.c_uint32), ("max_pending", ctypes.c_uint32),
+                ("use_graphs", ctypes.c_int32)]
+
+
+class NesRequest(ctypes.Structure):
+    _fields_ = [("nviews", ctypes.c_uint32), ("views", NesView * 2)]
+
+
+class NesResult(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_uint64), ("status", ctypes.c_int32), ("nviews", ctypes.c_uint32),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("linesize", ctypes.c_int32 * 3),
+                ("y_dev", ctypes.c_void_p * 2), ("u_dev", ctypes.c_void_p * 2), ("v_dev", ctypes.c_void_p * 2),
+                ("depth_mm_dev", ctypes.c_void_p * 2), ("latency_ms", ctypes.c_double),
+                ("batch_id", ctypes.c_uint64), ("batch_requests", ctypes.c_uint32),
+                ("batch_views", ctypes.c_uint32)]
+
+
+class NesServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "rejected", "completed", "batches", "pixels",
+                                               "samples", "graph_instantiations", "graph_updates",
+                                               "budget_used_bytes")]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _SZ = ctypes.c_size_t
@@ -86,6 +111,14 @@ _SIGS = {
     "nes_rebuild_occupancy": (_I, [_P, ctypes.c_float]),
     "nes_last_sample_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "nes_render_view_noalloc": (_I, [_P, ctypes.c_uint32, _P, _P, ctypes.POINTER(NesView), _P, _P, _P]),
+    "nes_server_config_default": (None, [ctypes.POINTER(NesServerConfig)]),
+    "nes_server_create": (_I, [_P, ctypes.POINTER(NesServerConfig), ctypes.POINTER(_P)]),
+    "nes_server_destroy": (None, [_P]),
+    "nes_submit": (_I, [_P, ctypes.POINTER(NesRequest), ctypes.POINTER(ctypes.c_uint64)]),
+    "nes_wait": (_I, [_P, ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(NesResult)]),
+    "nes_release": (_I, [_P, ctypes.c_uint64]),
+    "nes_server_stats_get": (_I, [_P, ctypes.POINTER(NesServerStats)]),
+    "nes_copy_to_host": (_I, [_P, _P, _SZ]),
     "nes_set_profiling": (_I, [_P, _I]),
     "nes_last_timings": (_I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "nes_scene_generate": (_I, [ctypes.c_uint64, ctypes.c_uint32, _P, _P]),
@@ -326,3 +359,75 @@ def stereo_pair(pose, ipd):
             m[row * 4 + 3] = pose[row * 4 + 3] + sgn * ipd * pose[row * 4 + 0]
         out.append(m)
     return out
+
+
+class Server:
+    """Continuously batched serving loop on one Renderer (nes_server_*)."""
+
+    def __init__(self, renderer, **kw):
+        self.lib = load()
+        self.renderer = renderer
+        cfg = NesServerConfig()
+        self.lib.nes_server_config_default(ctypes.byref(cfg))
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        self.cfg = cfg
+        h = _P()
+        check(self.lib.nes_server_create(renderer.h, ctypes.byref(cfg), ctypes.byref(h)), "nes_server_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.nes_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, views):
+        """Admits a mono ([view]) or stereo ([left, right]) request; returns
+        its ticket, or None when it was dropped (budget / queue full)."""
+        req = NesRequest()
+        req.nviews = len(views)
+        for i, v in enumerate(views):
+            req.views[i] = v
+        t = ctypes.c_uint64(0)
+        rc = self.lib.nes_submit(self.h, ctypes.byref(req), ctypes.byref(t))
+        if rc == NES_EAGAIN:
+            return None
+        check(rc, "nes_submit")
+        return t.value
+
+    def wait(self, ticket, timeout_ns=-1):
+        res = NesResult()
+        rc = self.lib.nes_wait(self.h, ticket, timeout_ns, ctypes.byref(res))
+        if rc == NES_ETIMEDOUT:
+            return None
+        check(rc, "nes_wait")
+        return res
+
+    def release(self, ticket):
+        check(self.lib.nes_release(self.h, ticket), "nes_release")
+
+    def stats(self):
+        st = NesServerStats()
+        check(self.lib.nes_server_stats_get(self.h, ctypes.byref(st)), "nes_server_stats_get")
+        return {n: getattr(st, n) for n, _ in NesServerStats._fields_}
+
+    def fetch(self, res, view=0):
+        """Copies one served view to host: (y, u, v, depth_mm) numpy arrays."""
+        import numpy as np
+        h, ls = res.height, list(res.linesize)
+        ch = (h + 1) // 2
+        out = []
+        for ptr, n in ((res.y_dev[view], ls[0] * h), (res.u_dev[view], ls[1] * ch), (res.v_dev[view], ls[2] * ch)):
+            a = np.empty(n, np.uint8)
+            check(self.lib.nes_copy_to_host(a.ctypes.data, ptr, n), "nes_copy_to_host")
+            out.append(a)
+        d = np.empty(res.width * h, np.uint16)
+        check(self.lib.nes_copy_to_host(d.ctypes.data, res.depth_mm_dev[view], d.nbytes), "nes_copy_to_host")
+        out.append(d)
+        return out
