@@ -49,6 +49,8 @@ def parse_args():
     p.add_argument("--precision", choices=["auto", "fp32", "tc"], default="auto")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=None)
+    p.add_argument("--no-extras", action="store_true", help="skip the stereo and serving sections")
+    p.add_argument("--serve-seconds", type=float, default=2.0)
     p.add_argument("--width", type=int, default=1920, help="smaller sizes only for profiling captures")
     p.add_argument("--height", type=int, default=1080)
     return p.parse_args()
@@ -296,12 +298,199 @@ def run_ours(args):
                     "e2e_mrays": round(v["e2e"]["mrays"], 3), "p99_ms": round(v["e2e"]["p99_ms"], 3)}
                    if "mrays" in v else v) for k, v in results.items()},
     }
+    if world == 1 and not args.no_extras:
+        line["stereo"] = run_stereo(dev, min(args.steps, 20))
+        line["serving"] = run_serving(dev, args.serve_seconds)
     if not args.no_cpu_baseline:
         per = (W * H) // 32
-        mrays, secs, px, threads = cpu_sample(poses, [per], 7)
-        line["cpu_baseline"] = {"value": round(mrays, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                                "sample": "%d random pixels of one 1920x1080 request (FP64 oracle, %.1f s)" % (px, secs)}
+        cb = cpu_baseline_with_parity(dev, poses[0], per)
+        line["cpu_baseline"] = cb
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_with_parity(dev, pose, npx):
+    """The FP64 oracle timed on a random pixel sample of one request; the same
+    pixels of the tensor-core render are compared against it (PSNR, depth)."""
+    import numpy as np
+    import torch
+    import nes
+    f = nes.focal_from_fov(W, FOV)
+    with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=W * H, device=dev.index) as r:
+        rgb = torch.empty(W * H * 3, device=dev)
+        dep = torch.empty(W * H, device=dev)
+        r.render_views([nes.make_view(pose, W, H, f)], [rgb.data_ptr()], [dep.data_ptr()])
+        torch.cuda.synchronize()
+        g_rgb = rgb.cpu().numpy().reshape(-1, 3)
+        g_dep = dep.cpu().numpy()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    scene = oracle.Scene(0, 19)
+    pix = np.random.default_rng(7).choice(W * H, npx, replace=False).astype(np.int32)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    orgb, odep, _ = scene.render(pose, W, H, f, pixels=pix, nthreads=threads)
+    secs = time.perf_counter() - t0
+    mse = float(np.mean((g_rgb[pix] - orgb) ** 2))
+    return {"value": round(npx / secs / 1e6, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": "%d random pixels of one 1920x1080 request (FP64 oracle, %.1f s)" % (npx, secs),
+            "parity_fp16_tc": {"psnr_db": round(10 * math.log10(1.0 / mse), 2) if mse > 0 else None,
+                               "max_abs_depth_err": float(np.abs(g_dep[pix] - odep).max()), "pixels": npx}}
+
+
+def run_stereo(dev, steps):
+    """Precision-form workload: stereo 2x1920x1832 per request, 100 deg FOV,
+    IPD 0.063, poses on the r = 1.2..2.0 shell; per-request device time of
+    raygen + march + RGB24 + YUV420P + depth packing for both eyes."""
+    import torch
+    import nes
+    SW, SH = 1920, 1832
+    f = nes.focal_from_fov(SW, 100.0)
+    poses = nes.shell_poses(0, 200, 1.2, 2.0)
+    ls = nes.linesizes(SW)
+    ch = (SH + 1) // 2
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    lib = nes.load()
+    bufs = []
+    for _ in range(2):
+        bufs.append(dict(rgb=torch.empty(SW * SH * 3, device=dev), dep=torch.empty(SW * SH, device=dev),
+                         rgb8=torch.empty(SW * SH * 3, dtype=torch.uint8, device=dev),
+                         yuv=torch.empty(ls[0] * SH + 2 * ls[1] * ch, dtype=torch.uint8, device=dev),
+                         dmm=torch.empty(SW * SH, dtype=torch.int16, device=dev)))
+    with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=2 * SW * SH, device=dev.index) as r:
+        def request(i):
+            eyes = nes.stereo_pair(poses[i % len(poses)], 0.063)
+            r.render_views([nes.make_view(m, SW, SH, f) for m in eyes], [b["rgb"].data_ptr() for b in bufs],
+                           [b["dep"].data_ptr() for b in bufs], sptr)
+            for b in bufs:
+                y = b["yuv"].data_ptr()
+                nes.check(lib.nes_rgb_to_rgb24(b["rgb"].data_ptr(), SW * SH * 3, b["rgb8"].data_ptr(), sptr), "rgb24")
+                nes.rgb24_to_yuv420p(b["rgb8"].data_ptr(), SW, SH, SW * 3, y, y + ls[0] * SH,
+                                     y + ls[0] * SH + ls[1] * ch, ls, sptr)
+                nes.depth_pack_u16mm(b["dep"].data_ptr(), SW * SH, b["dmm"].data_ptr(), sptr)
+        for i in range(3):
+            request(i)
+        torch.cuda.synchronize()
+        ms, samples = [], []
+        for i in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            request(i)
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+            samples.append(r.last_sample_count())
+    ms_sorted = sorted(ms)
+    return {"workload": "stereo 2x1920x1832, 100 deg FOV, IPD 0.063, poses on r=1.2..2.0 shell, FP16 tcgen05",
+            "requests": steps, "p50_ms": round(ms_sorted[len(ms) // 2], 3),
+            "p99_ms": round(ms_sorted[min(len(ms) - 1, int(math.ceil(0.99 * len(ms))) - 1)], 3),
+            "mrays": round(2 * SW * SH * steps / (sum(ms) / 1e3) / 1e6, 3),
+            "samples_per_pixel": round(statistics.mean(samples) / (2 * SW * SH), 2),
+            "timing": "CUDA events around each request (device time, pose already on the host)"}
+
+
+def random_walk_poses(seed, n, rmin=1.2, rmax=2.0, jitter_deg=0.5):
+    """Seeded random walk on the shell: each pose turns the eye direction by
+    a random rotation of std jitter_deg and moves the radius a little."""
+    import numpy as np
+    import nes
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    r = 0.5 * (rmin + rmax)
+    out = []
+    for _ in range(n):
+        axis = rng.normal(size=3)
+        axis -= axis.dot(d) * d
+        axis /= np.linalg.norm(axis)
+        ang = math.radians(jitter_deg) * rng.normal()
+        d = d * math.cos(ang) + np.cross(axis, d) * math.sin(ang)
+        d /= np.linalg.norm(d)
+        r = float(np.clip(r + 0.005 * rng.normal(), rmin, rmax))
+        out.append(nes.look_at(tuple(0.5 + r * d)))
+    return out
+
+
+def run_serving(dev, seconds):
+    """Serving form: open-loop Poisson arrivals, resolutions mixed uniformly
+    over mono 640x360, 1280x720, 1920x1080 and stereo 2x1920x1832, random-walk
+    poses; latency = submit -> YUV + depth ready on the device."""
+    import threading as th
+    import numpy as np
+    import nes
+    res = [(640, 360, False), (1280, 720, False), (1920, 1080, False), (1920, 1832, True)]
+    out = {}
+    with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=2 * 1920 * 1832, device=dev.index) as r:
+        srv = nes.Server(r, max_inflight_batches=2, max_batch_pixels=2 * 1920 * 1832,
+                         hbm_budget_bytes=80 << 30, max_pending=16)
+        try:
+            for rate in (90, 360, 720):
+                rng = np.random.default_rng(rate)
+                n = int(rate * seconds)
+                gaps = rng.exponential(1.0 / rate, n)
+                kinds = rng.integers(0, 4, n)
+                poses = random_walk_poses(rate, n)
+                tickets, lock = [], th.Lock()
+                done = th.Event()
+                lat, pix = [], [0]
+
+                def collect():
+                    i = 0
+                    while True:
+                        with lock:
+                            item = tickets[i] if i < len(tickets) else None
+                        if item is None:
+                            if done.is_set():
+                                with lock:
+                                    if i >= len(tickets):
+                                        return
+                                continue
+                            time.sleep(0.0005)
+                            continue
+                        t, px = item
+                        res_ = srv.wait(t)
+                        lat.append(res_.latency_ms)
+                        pix[0] += px
+                        srv.release(t)
+                        i += 1
+
+                col = th.Thread(target=collect)
+                col.start()
+                dropped = 0
+                t0 = time.perf_counter()
+                due = t0
+                for i in range(n):
+                    due += gaps[i]
+                    while time.perf_counter() < due:
+                        time.sleep(max(0.0, min(0.001, due - time.perf_counter())))
+                    w, h, stereo = res[kinds[i]]
+                    f = nes.focal_from_fov(w, 100.0 if stereo else 90.0)
+                    mats = nes.stereo_pair(poses[i], 0.063) if stereo else [poses[i]]
+                    t = srv.submit([nes.make_view(m, w, h, f) for m in mats])
+                    if t is None:
+                        dropped += 1
+                    else:
+                        with lock:
+                            tickets.append((t, w * h * len(mats)))
+                done.set()
+                col.join()
+                wall = time.perf_counter() - t0
+                ls = sorted(lat)
+                out[str(rate)] = {"offered": n, "completed": len(lat), "dropped": dropped,
+                                  "p50_ms": round(ls[len(ls) // 2], 3) if ls else None,
+                                  "p99_ms": round(ls[min(len(ls) - 1, int(math.ceil(0.99 * len(ls))) - 1)], 3)
+                                  if ls else None,
+                                  "mrays": round(pix[0] / wall / 1e6, 3)}
+            st = srv.stats()
+        finally:
+            srv.close()
+    out["workload"] = ("Poisson arrivals for %.1f s per rate; mono 640x360 / 1280x720 / 1920x1080 and stereo "
+                       "2x1920x1832 uniformly; random-walk poses on the r=1.2..2.0 shell (0.5 deg jitter); "
+                       "FP16 tcgen05; 2 batches in flight; latency = submit -> YUV+depth on device" % seconds)
+    out["batches"] = st["batches"]
+    out["graph_instantiations"] = st["graph_instantiations"]
+    out["graph_updates"] = st["graph_updates"]
+    return out
 
 
 def main():
