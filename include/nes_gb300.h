@@ -107,6 +107,17 @@ size_t nes_rendered_frame_capacity(uint32_t width, uint32_t height);
 int nes_render(nes_ctx *ctx, const uint8_t *request, size_t request_len, uint8_t *frame_out,
                size_t frame_cap, size_t *frame_len);
 
+/* Renderer endpoint for an unmodified neserver (`--renderer ip:port`):
+ * listens on bind_addr:port (port 0 picks a free one, reported in
+ * *bound_port) and answers each connection's length-prefixed FrameRequests
+ * with RenderedFrames through nes_render, exactly the framing of
+ * socket_send_blocking_lpf / socket_receive_blocking_lpf (src/server.cpp:46-112).
+ * Blocks until *stop becomes nonzero (checked every 100 ms), then closes the
+ * listener, finishes the open connections and returns; *frames_served counts
+ * answered requests.  Negative errno on socket errors. */
+int nes_tcp_serve(nes_ctx *ctx, const char *bind_addr, uint16_t port, const volatile int *stop,
+                  uint16_t *bound_port, uint64_t *frames_served);
+
 /* Device-native render of n views in one batch (rays of all views share
  * one march).  rgb_dev[i]: W*H*3 floats (HWC), depth_dev[i]: W*H floats
  * (expected depth, 0 for rays that miss); either may be NULL. */

@@ -119,6 +119,8 @@ _SIGS = {
     "nes_release": (_I, [_P, ctypes.c_uint64]),
     "nes_server_stats_get": (_I, [_P, ctypes.POINTER(NesServerStats)]),
     "nes_copy_to_host": (_I, [_P, _P, _SZ]),
+    "nes_tcp_serve": (_I, [_P, ctypes.c_char_p, ctypes.c_uint16, ctypes.POINTER(ctypes.c_int),
+                           ctypes.POINTER(ctypes.c_uint16), ctypes.POINTER(ctypes.c_uint64)]),
     "nes_set_profiling": (_I, [_P, _I]),
     "nes_last_timings": (_I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "nes_scene_generate": (_I, [ctypes.c_uint64, ctypes.c_uint32, _P, _P]),
@@ -359,6 +361,36 @@ def stereo_pair(pose, ipd):
             m[row * 4 + 3] = pose[row * 4 + 3] + sgn * ipd * pose[row * 4 + 0]
         out.append(m)
     return out
+
+
+class TcpEndpoint:
+    """nes_tcp_serve in a background thread: the renderer endpoint neserver
+    connects to with --renderer host:port."""
+
+    def __init__(self, renderer, port=0, bind="127.0.0.1"):
+        import threading
+        import time
+        self.lib = load()
+        self.stop = ctypes.c_int(0)
+        self.port = ctypes.c_uint16(0)
+        self.served = ctypes.c_uint64(0)
+        self.rc = None
+
+        def run():
+            self.rc = self.lib.nes_tcp_serve(renderer.h, bind.encode(), port, ctypes.byref(self.stop),
+                                             ctypes.byref(self.port), ctypes.byref(self.served))
+        self.thread = threading.Thread(target=run, daemon=True)
+        self.thread.start()
+        t0 = time.time()
+        while self.port.value == 0 and self.rc is None and time.time() - t0 < 10:
+            time.sleep(0.01)
+        if self.port.value == 0:
+            raise NesError(self.rc if self.rc is not None else NES_ETIMEDOUT, "nes_tcp_serve")
+
+    def close(self):
+        self.stop.value = 1
+        self.thread.join()
+        return self.served.value
 
 
 class Server:

@@ -17,6 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.normpath(os.path.join(HERE, "..", "include"))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnes_gb300.so")
+SERVER_BIN = os.path.join(HERE, "nes_render_server")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -40,6 +41,8 @@ def _stamp(srcs):
         with open(full, "rb") as f:
             h.update(p.encode())
             h.update(f.read())
+    with open(os.path.join(HERE, "render_server.cpp"), "rb") as f:
+        h.update(f.read())
     h.update(" ".join(CU_FLAGS).encode())
     return h.hexdigest()
 
@@ -65,7 +68,7 @@ def build(force=False, verbose=False):
     srcs = _sources()
     stamp = _stamp(srcs)
     stamp_file = os.path.join(BUILD, "stamp")
-    if not force and os.path.exists(LIB) and os.path.exists(stamp_file):
+    if not force and os.path.exists(LIB) and os.path.exists(SERVER_BIN) and os.path.exists(stamp_file):
         with open(stamp_file) as f:
             if f.read() == stamp:
                 return LIB
@@ -77,6 +80,12 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    # The renderer endpoint for an unmodified neserver, linked to the library.
+    cmd = ["g++", "-O2", "-std=c++17", "-I", INCLUDE, os.path.join(HERE, "render_server.cpp"), "-o", SERVER_BIN,
+           "-L", HERE, "-lnes_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("render server link failed\n%s%s" % (r.stdout, r.stderr))
     with open(stamp_file, "w") as f:
         f.write(stamp)
     return LIB

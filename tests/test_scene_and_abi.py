@@ -69,6 +69,19 @@ def test_create_without_gpu_fails_cleanly(nes_lib):
     assert e.value.code == nes_lib.NES_ENODEV
 
 
+def test_render_server_binary_fails_cleanly_without_gpu(nes_lib):
+    import os
+    import subprocess
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import nes_build
+    r = subprocess.run([nes_build.SERVER_BIN, "--port", "0"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "no usable CUDA device" in r.stderr
+    r = subprocess.run([nes_build.SERVER_BIN, "--bogus", "1"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
+
+
 def test_focal_and_capacity(nes_lib):
     assert nes_lib.focal_from_fov(1920, 90.0) == pytest.approx(960.0, rel=1e-6)
     assert nes_lib.focal_from_fov(256, 90.0) == np.float32(128.0)

@@ -104,6 +104,54 @@ def test_render_pb_errors(r32, nes_lib):
     assert lib.nes_render(r32.h, huge, len(huge), None, 0, ctypes.byref(n)) == nes_lib.NES_EINVAL
 
 
+def _lpf_send(sock, payload):
+    import struct
+    sock.sendall(struct.pack("=Q", len(payload)) + payload)  # host-endian size_t, src/server.cpp:46-60
+
+
+def _lpf_recv(sock):
+    import struct
+
+    def exact(n):
+        buf = b""
+        while len(buf) < n:
+            chunk = sock.recv(n - len(buf))
+            if not chunk:
+                raise EOFError
+            buf += chunk
+        return buf
+    (n,) = struct.unpack("=Q", exact(8))
+    return exact(n)
+
+
+def test_tcp_endpoint_speaks_the_renderer_protocol(r32, nes_lib):
+    """Acts as neserver's socket_client_thread (src/server.cpp:132-209):
+    alternating left/right requests on one connection, a second concurrent
+    connection, and a malformed request that closes its connection."""
+    import socket
+    ep = nes_lib.TcpEndpoint(r32)
+    try:
+        poses = nes_lib.shell_poses(8, 4, 1.5, 1.5)
+        a = socket.create_connection(("127.0.0.1", ep.port.value), timeout=30)
+        b = socket.create_connection(("127.0.0.1", ep.port.value), timeout=30)
+        for i, M in enumerate(poses[:3]):
+            req = frame_request(i, i % 2 == 0, 48, 32, M)
+            _lpf_send(a, req)
+            got = _lpf_recv(a)
+            assert got == r32.render(req)
+        req = frame_request(99, False, 24, 16, poses[3])
+        _lpf_send(b, req)
+        assert _lpf_recv(b) == r32.render(req)
+        _lpf_send(b, b"\x12\x10\x18\x01")  # truncated camera: the endpoint closes the connection
+        with pytest.raises((EOFError, ConnectionError)):
+            _lpf_recv(b)
+        a.close()
+        b.close()
+    finally:
+        served = ep.close()
+    assert ep.rc == 0 and served == 4
+
+
 def test_render_yuv_end_to_end(r32, cuda, nes_lib, oracle_mod):
     torch = cuda
     M = nes_lib.shell_poses(0, 100, 1.5, 1.5)[3]
