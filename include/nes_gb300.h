@@ -241,6 +241,23 @@ int nes_gray8_to_yuv420p(const uint8_t *gray_dev, int width, int height, int gra
                          uint8_t *y_dev, uint8_t *u_dev, uint8_t *v_dev, const int linesize[3],
                          void *stream);
 
+/* Debug text overlay into an RGB24 frame on the device, before conversion:
+ * RenderTextContext::render_string_to_frame (src/base/video/render_text.cc:35-111)
+ * with the same five anchors (margin 50, box 300x100), '\n' = back to the
+ * anchor column and 20 px down, covered pixels set to white, clipped to the
+ * frame.  Glyphs are this library's 5x7 font at 2x (10x14 px, 12 px advance,
+ * baseline at the pen) for ' ', + - . : = 0-9 a-z; other characters advance
+ * without drawing.  At most 512 drawn characters per call. */
+enum nes_text_anchor {
+  NES_TEXT_LEFT_TOP = 0,
+  NES_TEXT_LEFT_BOTTOM = 1,
+  NES_TEXT_RIGHT_TOP = 2,
+  NES_TEXT_RIGHT_BOTTOM = 3,
+  NES_TEXT_CENTER = 4
+};
+int nes_overlay_text(uint8_t *rgb_dev, int width, int height, int linesize, const char *text, int anchor,
+                     void *stream);
+
 /* FP32 depth (scene units = metres) -> uint16 millimetres, round half up,
  * NaN/negative -> 0, saturating at 65535. */
 int nes_depth_pack_u16mm(const float *depth_dev, size_t n, uint16_t *out_dev, void *stream);

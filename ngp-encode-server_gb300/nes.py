@@ -119,6 +119,7 @@ _SIGS = {
     "nes_release": (_I, [_P, ctypes.c_uint64]),
     "nes_server_stats_get": (_I, [_P, ctypes.POINTER(NesServerStats)]),
     "nes_copy_to_host": (_I, [_P, _P, _SZ]),
+    "nes_overlay_text": (_I, [_P, _I, _I, _I, ctypes.c_char_p, _I, _P]),
     "nes_tcp_serve": (_I, [_P, ctypes.c_char_p, ctypes.c_uint16, ctypes.POINTER(ctypes.c_int),
                            ctypes.POINTER(ctypes.c_uint16), ctypes.POINTER(ctypes.c_uint64)]),
     "nes_set_profiling": (_I, [_P, _I]),

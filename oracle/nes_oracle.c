@@ -625,3 +625,65 @@ void oracle_rgb_to_rgb24(const float *rgb, long n, uint8_t *out) {
     out[i] = (uint8_t)(uint32_t)r;
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* Debug text overlay (RenderTextContext::render_string_to_frame,      */
+/* src/base/video/render_text.cc:35-111): five anchors with margin 50  */
+/* and a 300x100 box, '\n' = anchor column and 20 px down, covered      */
+/* pixels set to white, clipped.  Glyphs: 5x7 dot matrix drawn at 2x,   */
+/* 12 px advance, bottom row on the pen's baseline.                     */
+/* ------------------------------------------------------------------ */
+static const struct {
+  char c;
+  unsigned char r[7];
+} OR_GLYPHS[] = {
+    {'0', {14, 17, 19, 21, 25, 17, 14}}, {'1', {4, 12, 4, 4, 4, 4, 14}},     {'2', {14, 17, 1, 2, 4, 8, 31}},
+    {'3', {30, 1, 1, 14, 1, 1, 30}},     {'4', {2, 6, 10, 18, 31, 2, 2}},    {'5', {31, 16, 30, 1, 1, 17, 14}},
+    {'6', {6, 8, 16, 30, 17, 17, 14}},   {'7', {31, 1, 2, 4, 8, 8, 8}},      {'8', {14, 17, 17, 14, 17, 17, 14}},
+    {'9', {14, 17, 17, 15, 1, 2, 12}},   {'+', {0, 4, 4, 31, 4, 4, 0}},      {'-', {0, 0, 0, 31, 0, 0, 0}},
+    {'.', {0, 0, 0, 0, 0, 12, 12}},      {':', {0, 12, 12, 0, 12, 12, 0}},   {'=', {0, 0, 31, 0, 31, 0, 0}},
+    {'a', {0, 0, 14, 1, 15, 17, 15}},    {'b', {16, 16, 22, 25, 17, 17, 30}}, {'c', {0, 0, 14, 16, 16, 17, 14}},
+    {'d', {1, 1, 13, 19, 17, 17, 15}},   {'e', {0, 0, 14, 17, 31, 16, 14}},  {'f', {6, 9, 8, 28, 8, 8, 8}},
+    {'g', {0, 15, 17, 17, 15, 1, 14}},   {'h', {16, 16, 22, 25, 17, 17, 17}}, {'i', {4, 0, 12, 4, 4, 4, 14}},
+    {'j', {2, 0, 6, 2, 2, 18, 12}},      {'k', {16, 16, 18, 20, 24, 20, 18}}, {'l', {12, 4, 4, 4, 4, 4, 14}},
+    {'m', {0, 0, 26, 21, 21, 17, 17}},   {'n', {0, 0, 22, 25, 17, 17, 17}},  {'o', {0, 0, 14, 17, 17, 17, 14}},
+    {'p', {0, 0, 30, 17, 30, 16, 16}},   {'q', {0, 0, 13, 19, 15, 1, 1}},    {'r', {0, 0, 22, 25, 16, 16, 16}},
+    {'s', {0, 0, 14, 16, 14, 1, 30}},    {'t', {8, 8, 28, 8, 8, 9, 6}},      {'u', {0, 0, 17, 17, 17, 19, 13}},
+    {'v', {0, 0, 17, 17, 17, 10, 4}},    {'w', {0, 0, 17, 17, 21, 21, 10}},  {'x', {0, 0, 17, 10, 4, 10, 17}},
+    {'y', {0, 0, 17, 17, 15, 1, 14}},    {'z', {0, 0, 31, 2, 4, 8, 31}},
+};
+
+static const unsigned char *or_glyph(char c) {
+  for (size_t i = 0; i < sizeof(OR_GLYPHS) / sizeof(OR_GLYPHS[0]); i++)
+    if (OR_GLYPHS[i].c == c) return OR_GLYPHS[i].r;
+  return NULL;
+}
+
+void oracle_overlay_text(uint8_t *rgb, int w, int h, int ls, const char *text, int anchor) {
+  const int x_box = 300, y_box = 100, margin = 50;
+  int pen_x = margin, pen_y = margin;
+  if (anchor == 1) { pen_x = margin; pen_y = h - y_box + margin; }
+  else if (anchor == 2) { pen_x = w - x_box + margin; pen_y = margin; }
+  else if (anchor == 3) { pen_x = w - x_box + margin; pen_y = h - y_box + margin; }
+  else if (anchor == 4) { pen_x = w / 2 - x_box; pen_y = h / 2 - y_box; }
+  const int x0 = pen_x;
+  for (const char *c = text; *c; c++) {
+    if (*c == '\n') {
+      pen_x = x0;
+      pen_y += 20;
+      continue;
+    }
+    const unsigned char *g = or_glyph(*c);
+    if (g) {
+      for (int py = 0; py < 14; py++)
+        for (int px = 0; px < 10; px++) {
+          if (!((g[py / 2] >> (4 - px / 2)) & 1)) continue;
+          int X = pen_x + px, Y = pen_y - 14 + py;
+          if (X < 0 || Y < 0 || X >= w || Y >= h) continue;
+          uint8_t *q = rgb + (size_t)Y * ls + (size_t)X * 3;
+          q[0] = q[1] = q[2] = 255;
+        }
+    }
+    pen_x += 12;
+  }
+}

@@ -38,7 +38,15 @@ _SIGS = {
     "oracle_depth_to_gray8": (None, [_P, ctypes.c_long, ctypes.c_float, _P]),
     "oracle_rgb_to_rgb24": (None, [_P, ctypes.c_long, _P]),
     "oracle_stream_key": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint32]),
+    "oracle_overlay_text": (None, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
 }
+
+
+def overlay_text(rgb, w, h, ls, text, anchor):
+    """Draws text into a copy of the RGB24 frame (uint8, h*ls bytes)."""
+    out = np.ascontiguousarray(rgb, dtype=np.uint8).copy()
+    load().oracle_overlay_text(out.ctypes.data, w, h, ls, text.encode(), anchor)
+    return out
 
 _lib = None
 

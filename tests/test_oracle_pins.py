@@ -178,6 +178,21 @@ def test_oracle_matches_golden_render(scene0):
     assert np.allclose(depth, g["depth"], rtol=0, atol=1e-12)
 
 
+def test_overlay_glyph_placement(oracle_mod):
+    # '1' (rows 00100 01100 00100 00100 00100 00100 01110) at 2x, pen at the
+    # left-top anchor (50, 50), bottom row on the baseline: 10 set bits -> 40
+    # white pixels, top-left set pixel at (54, 36).
+    w = h = 100
+    out = oracle_mod.overlay_text(np.zeros(h * w * 3, np.uint8), w, h, w * 3, "1", 0).reshape(h, w, 3)
+    white = np.argwhere(out[:, :, 0] == 255)
+    assert len(white) == 40 and np.all(out[out[:, :, 0] == 255] == 255)
+    assert white[:, 0].min() == 36 and white[:, 0].max() == 49
+    assert tuple(white[0]) == (36, 54)
+    # '\n' returns to the anchor column 20 px lower; unknown glyphs only advance.
+    a = oracle_mod.overlay_text(np.zeros(h * w * 3, np.uint8), w, h, w * 3, "#\n1", 0).reshape(h, w, 3)
+    assert np.argwhere(a[:, :, 0] == 255)[:, 0].min() == 56
+
+
 def test_oracle_matches_golden_yuv(oracle_mod):
     g = np.load(os.path.join(GOLDEN, "yuv_small.npz"))
     w, h, ls = int(g["w"]), int(g["h"]), [int(v) for v in g["ls"]]
