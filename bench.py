@@ -54,6 +54,7 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-extras", action="store_true", help="skip the stereo and serving sections")
     p.add_argument("--serve-seconds", type=float, default=2.0)
+    p.add_argument("--train-steps", type=int, default=20, help="refit steps timed in the training section")
     p.add_argument("--width", type=int, default=1920, help="smaller sizes only for profiling captures")
     p.add_argument("--height", type=int, default=1080)
     return p.parse_args()
@@ -307,6 +308,8 @@ def run_ours(args):
     if world == 1 and not args.no_extras:
         line["stereo"] = run_stereo(dev, min(args.steps, 20))
         line["serving"] = run_serving(dev, args.serve_seconds)
+        if args.train_steps > 0:
+            line["training"] = run_training(dev, args.train_steps)
     if not args.no_cpu_baseline:
         per = (W * H) // 32
         cb = cpu_baseline_with_parity(dev, poses[0], per)
@@ -393,6 +396,65 @@ def run_stereo(dev, steps):
             "mrays": round(2 * SW * SH * steps / (sum(ms) / 1e3) / 1e6, 3),
             "samples_per_pixel": round(statistics.mean(samples) / (2 * SW * SH), 2),
             "timing": "CUDA events around each request (device time, pose already on the host)"}
+
+
+def run_training(dev, steps, nviews=32, side=400, batch=1 << 18):
+    """Refit workload: an FP32 teacher (seed 1, T=2^19) renders nviews
+    side x side targets from the r = 1.2..2.0 shell; an FP32 student (seed
+    2) takes Adam steps of `batch` rays (lr 1e-2, L2 RGB + 0.1 L2 depth).
+    Each step is synchronous; its device phases come from CUDA events on the
+    trainer's stream and the step time from the host clock around the call.
+    PSNR of the student against the teacher on a held-out view before and
+    after the timed steps."""
+    import numpy as np
+    import torch
+    import nes
+    f = nes.focal_from_fov(side, 60.0)
+    poses = nes.shell_poses(11, nviews + 1, 1.2, 2.0)
+    views = [nes.make_view(m, side, side, f) for m in poses[:nviews]]
+    held = nes.make_view(poses[nviews], side, side, f)
+    px = side * side
+    rgb = torch.empty((nviews * px, 3), device=dev)
+    dep = torch.empty(nviews * px, device=dev)
+    hr, hd = torch.empty((px, 3), device=dev), torch.empty(px, device=dev)
+    with nes.Renderer(precision=nes.PREC_FP32, seed=1, max_pixels=nviews * px, device=dev.index) as teacher:
+        teacher.render_views(views, [rgb[i * px:].data_ptr() for i in range(nviews)],
+                             [dep[i * px:].data_ptr() for i in range(nviews)])
+        teacher.render_views([held], [hr.data_ptr()], [hd.data_ptr()])
+        torch.cuda.synchronize()
+    sr, sd = torch.empty((px, 3), device=dev), torch.empty(px, device=dev)
+
+    def psnr(r):
+        r.render_views([held], [sr.data_ptr()], [sd.data_ptr()])
+        torch.cuda.synchronize()
+        mse = float(torch.mean((sr - hr) ** 2))
+        return round(10 * math.log10(1.0 / mse), 2) if mse > 0 else None
+
+    with nes.Renderer(precision=nes.PREC_FP32, seed=2, max_pixels=px, device=dev.index) as student:
+        p0 = psnr(student)
+        with nes.Trainer(student, batch_rays=batch) as tr:
+            tr.set_targets(views, rgb.data_ptr(), dep.data_ptr())
+            losses = [tr.step(1000 + i) for i in range(3)]  # warm-up steps (part of the refit)
+            wall, phases, samples = [], [], []
+            for i in range(steps):
+                t0 = time.perf_counter()
+                losses.append(tr.step(i))
+                wall.append(time.perf_counter() - t0)
+                phases.append(tr.last_timings())
+                samples.append(tr.last_samples())
+        p1 = psnr(student)
+    ms = 1e3 * statistics.median(wall)
+    fwd, bwd, adam = (statistics.median(p[k] for p in phases) for k in range(3))
+    return {"workload": "refit teacher seed 1 -> student seed 2, T=2^19, %d views %dx%d, %d rays/step, Adam lr 1e-2"
+                        % (nviews, side, side, batch),
+            "steps": steps, "ms_per_step": round(ms, 2), "mrays_per_s": round(batch / ms / 1e3, 3),
+            "samples_per_step": int(statistics.median(samples)),
+            "msamples_per_s": round(statistics.median(samples) / ms / 1e3, 1),
+            "phase_ms": {"forward": round(fwd, 2), "backward": round(bwd, 2), "adam": round(adam, 2)},
+            "loss": {"first": round(losses[0], 6), "last": round(losses[-1], 6),
+                     "curve": [round(v, 6) for v in losses[::max(1, len(losses) // 8)]]},
+            "held_out_psnr_db": {"before": p0, "after": p1},
+            "timing": "host clock around each synchronous step; phases from CUDA events"}
 
 
 def random_walk_poses(seed, n, rmin=1.2, rmax=2.0, jitter_deg=0.5):

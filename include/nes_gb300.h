@@ -226,6 +226,71 @@ int nes_server_stats_get(nes_server *srv, nes_server_stats *out);
  * host H.264 encoder (AVCodecContextManager::send_frame, src/encode.cpp:136). */
 int nes_copy_to_host(void *host_dst, const void *dev_src, size_t n);
 
+/* ---------------- differentiation: refit a scene to target renders ----------------
+ * No counterpart in neserver (which only renders); this is the training
+ * form of the renderer: a hand-written backward through the volume
+ * rendering (per-sample compositing adjoint from recorded sample states),
+ * the MLPs (per-sample backpropagation; weight gradients as split-K
+ * reductions over the samples) and the hash grid (atomic float2 scatter-add
+ * into an FP32 gradient table), then Adam on the student context's FP32
+ * table and weights.  The occupancy grid is left as it is (rebuild it with
+ * nes_rebuild_occupancy between steps where wanted).
+ * Loss per ray: |C - C*|^2 + depth_weight (D - D*)^2, averaged over the batch.
+ * Trainer calls hold the student context's lock; a nes_server must not be
+ * serving the same context meanwhile. */
+
+typedef struct nes_trainer nes_trainer;
+
+typedef struct nes_train_config {
+  uint32_t batch_rays;  /* rays per step (2^18 in the refit configuration) */
+  float lr, beta1, beta2, eps;
+  float depth_weight;
+} nes_train_config;
+
+/* lr 1e-2, betas (0.9, 0.99), eps 1e-15, depth weight 0.1, 2^18 rays. */
+void nes_train_config_default(nes_train_config *cfg);
+
+/* The student must be an NES_PREC_FP32 context; its table and weights are
+ * updated in place by the step calls.  batch_rays <= 2^20.  Device memory:
+ * 64 B per ray per march step (1024 steps) of scratch plus ~3.9 GB of
+ * per-sample staging and 4x the table for gradient and Adam moments. */
+int nes_trainer_create(nes_ctx *student, const nes_train_config *cfg, nes_trainer **out);
+void nes_trainer_destroy(nes_trainer *tr);
+
+/* Target images: nviews views (1..1024) with HWC FP32 RGB and FP32 depth on
+ * the device, concatenated view after view (pointers are kept, not copied). */
+int nes_trainer_set_targets(nes_trainer *tr, const nes_view *views, int nviews, const float *rgb_dev,
+                            const float *depth_dev);
+
+/* One step: samples batch_rays (view, pixel) pairs from the seed, computes
+ * the loss and gradients, applies Adam.  *loss = mean loss before the update. */
+int nes_trainer_step(nes_trainer *tr, uint64_t seed, double *loss);
+
+/* One step on the listed rays (n pairs of int32 view, pixel on the host). */
+int nes_trainer_step_rays(nes_trainer *tr, const int32_t *rays, int n, double *loss);
+
+/* Loss and gradient of the mean loss over the listed rays (rays: n pairs of
+ * int32 view, pixel on the host), without updating anything.  Gradient
+ * outputs (host, may be NULL): table 16*T*2 floats, weights 9,408 floats
+ * (layout of nes_scene_generate). */
+int nes_trainer_grad(nes_trainer *tr, const int32_t *rays, int n, double *loss, float *grad_table,
+                     float *grad_weights);
+
+/* The same loss evaluated in FP64 on the GPU with one parameter perturbed by
+ * delta (which: 0 table, 1 weights blob; index into that array), for
+ * central finite-difference checks. */
+int nes_trainer_loss_fp64(nes_trainer *tr, const int32_t *rays, int n, int which, uint64_t index, double delta,
+                          double *loss);
+
+/* Samples evaluated (and backpropagated) by the last loss/gradient pass. */
+uint64_t nes_trainer_last_samples(const nes_trainer *tr);
+
+/* Device time of the last step's phases from CUDA events on the trainer's
+ * stream: forward march + compositing adjoint, backward (recompute,
+ * backpropagation, table scatter, weight-gradient reductions), Adam.
+ * NES_EAGAIN before the first step. */
+int nes_trainer_last_timings(const nes_trainer *tr, float *forward_ms, float *backward_ms, float *adam_ms);
+
 /* ---------------- (ii) frame glue ---------------- */
 
 /* RGB24 -> YUV420P, BT.601 studio range, 2x2 chroma average (edge pixels

@@ -1,0 +1,816 @@
+// train.cu -- differentiation of the renderer and the Adam refit
+// (nes_trainer_* in include/nes_gb300.h).  neserver itself only renders;
+// this is the training form of the same field (refit configuration: teacher
+// scene seed 1, student seed 2, 2^18 rays per step, L2 on RGB + 0.1 L2 on
+// depth, Adam lr 1e-2, betas (0.9, 0.99), eps 1e-15).
+//
+// Per step:
+//  1. rays: (view, pixel) pairs (drawn from the step seed or given) -> the
+//     FP32 ray set-up of rendering, with the target colour and depth;
+//  2. forward (thread per ray): march once, keeping each evaluated sample's
+//     t, alpha, transmittance and colour in the ray's scratch row; loss;
+//     then walk the samples backwards carrying A = dL/dT_k for each one's
+//     compositing adjoint
+//        g_w = g_C . c_k + g_D t_k,   dL/dc_k = g_C w_k,
+//        dL/dsigma_k = dt T_{k+1} (g_w - A_{k+1}),
+//        A_k = g_w alpha_k + A_{k+1} (1 - alpha_k),   A_K = 0,
+//     with g_C = 2 (C - C*)/B and g_D = 2 lambda (D - D*)/B, written as a
+//     compact 32-byte record (position, ray, dsigma, dc).  The backward
+//     sweep keeps every term proportional to T_{k+1}; the equivalent
+//     forward form with suffix sums (C - prefix) cancels in FP32 late in
+//     the ray;
+//  3. backward (thread per record, in chunks): recompute the encoding and
+//     both MLPs, backpropagate, scatter-add the encoding gradient into the
+//     FP32 gradient table with float2 atomics, and stage every layer's input
+//     activations and output deltas;
+//  4. weight gradients: per layer dW[out][in] += sum_s delta[s][out] act[s][in]
+//     over the chunk (dw_kernel, register-tiled split-K reduction);
+//  5. Adam on the table and the weights (bias-corrected); gradients zeroed.
+// An FP64 variant of the loss evaluates the same function with one parameter
+// perturbed, for central finite differences.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "ctx_internal.h"
+#include "kernels.h"
+#include "mlp32.cuh"
+#include "nes_gb300.h"
+
+using namespace nes;
+
+namespace {
+
+struct TrainView {
+  float M[12];
+  int W, H;
+  float focal;
+  int pad;
+  uint64_t offset;  // first pixel of this view in the concatenated targets
+};
+
+struct TrainRay {
+  float ox, oy, oz, ts;
+  float dx, dy, dz;
+  int n;                 // march steps (0: the ray misses the cube)
+  float tr, tg, tb, td;  // target colour and depth
+};
+
+struct ScratchSample {  // pass-1 state of one evaluated sample
+  float t, alpha, T, cr, cg, cb, pad0, pad1;  // T: transmittance before the sample
+};
+
+struct SampleRec {  // compacted sample with its compositing adjoint
+  float x, y, z;
+  uint32_t ray;
+  float dsigma, dcr, dcg, dcb;
+};
+
+// Per-sample staging rows of the weight-gradient reductions.
+constexpr int kStageFloats = kEnc + kHid + kCIn + kHid + kHid  // activations: enc, h1, cin, g1, g2
+                             + kHid + kDOut + kHid + kHid + 4;  // deltas: dh1, dout, dg1, dg2, dlogit(3)+pad
+struct Staging {
+  float *enc, *h1, *cin, *g1, *g2;       // [S][32], [S][64], [S][32], [S][64], [S][64]
+  float *dh1, *dout, *dg1, *dg2, *dlog;  // [S][64], [S][16], [S][64], [S][64], [S][4]
+};
+
+constexpr int kThreads = 128;
+constexpr uint32_t kErrBadRay = 2u, kErrOverflow = 3u;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Draw i of the step: view = low word mod nviews, pixel = high word mod W*H.
+__global__ void sample_pairs_kernel(uint64_t seed, int n, const TrainView* __restrict__ views, int nviews,
+                                    int2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t u = mix64(mix64(seed * 256ull + 7ull) + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull);
+  const int v = (int)((u & 0xffffffffull) % (uint64_t)nviews);
+  const uint64_t px = (uint64_t)views[v].W * views[v].H;
+  out[i] = make_int2(v, (int)((u >> 32) % px));
+}
+
+__global__ void make_rays_kernel(const int2* __restrict__ pairs, int n, const TrainView* __restrict__ views, int nviews,
+                                 const float* __restrict__ trgb, const float* __restrict__ tdep,
+                                 TrainRay* __restrict__ rays, uint32_t* __restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int2 p = pairs[i];
+  TrainRay r{};
+  if (p.x < 0 || p.x >= nviews || p.y < 0 || (uint64_t)p.y >= (uint64_t)views[p.x].W * views[p.x].H) {
+    atomicExch(err, kErrBadRay);
+    rays[i] = r;
+    return;
+  }
+  const TrainView& V = views[p.x];
+  float3 o, d;
+  float ts;
+  r.n = ray_setup(V.M, V.W, V.H, V.focal, p.y % V.W, p.y / V.W, o, d, ts);
+  r.ox = o.x; r.oy = o.y; r.oz = o.z; r.ts = ts;
+  r.dx = d.x; r.dy = d.y; r.dz = d.z;
+  const uint64_t q = V.offset + (uint64_t)p.y;
+  r.tr = trgb[q * 3 + 0];
+  r.tg = trgb[q * 3 + 1];
+  r.tb = trgb[q * 3 + 2];
+  r.td = tdep[q];
+  rays[i] = r;
+}
+
+// Forward + compositing adjoint, thread per ray.  Scratch row of ray i:
+// scratch[i * kMaxSteps, +K).  Compact records: one atomic per ray.
+__global__ void __launch_bounds__(kThreads)
+forward_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, ScratchSample* __restrict__ scratch,
+               SampleRec* __restrict__ recs, uint32_t capacity, uint32_t* __restrict__ cursor,
+               uint32_t* __restrict__ err, double* __restrict__ loss_sum, float depth_w, float inv_n) {
+  extern __shared__ float4 smem_raw[];
+  SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
+  load_weights32(W, sc.weights);
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float my_loss = 0.0f;
+  if (i < n) {
+    const TrainRay r = rays[i];
+    ScratchSample* row = scratch + (size_t)i * kMaxSteps;
+    float C[3] = {0.0f, 0.0f, 0.0f}, D = 0.0f;
+    int K = 0;
+    const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
+    if (r.n > 0) {
+      float sh[16];
+      sh16(d, sh);
+      float T = 1.0f;
+      for (int s = 0; s < r.n; ++s) {
+        const float t = fmaf((float)s + 0.5f, kDt, r.ts);
+        const float3 x = sample_pos(o, d, t);
+        if (!occupied(sc.occ, x)) continue;
+        float enc[kEnc];
+        encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
+        float dout[kDOut];
+        density_mlp32(W, enc, dout);
+        const float sigma = expf(dout[0] - 1.0f);
+        const float3 c = colour_mlp32(W, sh, dout);
+        const float alpha = -expm1f(-sigma * kDt);
+        const float w = T * alpha;
+        row[K] = ScratchSample{t, alpha, T, c.x, c.y, c.z, 0.0f, 0.0f};
+        ++K;
+        C[0] = fmaf(w, c.x, C[0]);
+        C[1] = fmaf(w, c.y, C[1]);
+        C[2] = fmaf(w, c.z, C[2]);
+        D = fmaf(w, t, D);
+        T -= w;
+        if (T < kTStop) break;
+      }
+    }
+    const float ec[3] = {C[0] - r.tr, C[1] - r.tg, C[2] - r.tb}, ed = D - r.td;
+    my_loss = (ec[0] * ec[0] + ec[1] * ec[1] + ec[2] * ec[2] + depth_w * ed * ed) * inv_n;
+    if (K > 0) {
+      const uint32_t base = atomicAdd(cursor, (uint32_t)K);
+      if (base + (uint32_t)K > capacity) {
+        atomicExch(err, kErrOverflow);
+      } else {
+        const float gC[3] = {2.0f * ec[0] * inv_n, 2.0f * ec[1] * inv_n, 2.0f * ec[2] * inv_n};
+        const float gD = 2.0f * depth_w * ed * inv_n;
+        float A = 0.0f;
+        for (int k = K - 1; k >= 0; --k) {
+          const ScratchSample q = row[k];
+          const float w = q.T * q.alpha;
+          const float T1 = q.T - w;
+          const float gw = fmaf(gC[0], q.cr, fmaf(gC[1], q.cg, fmaf(gC[2], q.cb, gD * q.t)));
+          const float dsig = kDt * T1 * (gw - A);
+          const float3 x = sample_pos(o, d, q.t);
+          recs[base + k] = SampleRec{x.x, x.y, x.z, (uint32_t)i, dsig, gC[0] * w, gC[1] * w, gC[2] * w};
+          A = fmaf(gw, q.alpha, A * (1.0f - q.alpha));
+        }
+      }
+    }
+  }
+  // One FP64 atomic per warp.
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) my_loss += __shfl_down_sync(0xffffffffu, my_loss, off);
+  if ((threadIdx.x & 31u) == 0 && my_loss != 0.0f) atomicAdd(loss_sum, (double)my_loss);
+}
+
+__device__ __forceinline__ float relu_d(float a, float g) { return a > 0.0f ? g : 0.0f; }
+
+// Backward, thread per record of the chunk [first, first + count).
+__global__ void __launch_bounds__(kThreads)
+backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t count, const TrainRay* __restrict__ rays,
+                const DevScene sc, Staging st, float2* __restrict__ gtable) {
+  extern __shared__ float4 smem_raw[];
+  SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
+  load_weights32(W, sc.weights);
+  __syncthreads();
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= count) return;
+  const SampleRec q = recs[first + s];
+  const TrainRay r = rays[q.ray];
+  const float3 x = make_float3(q.x, q.y, q.z);
+  float* enc_row = st.enc + (size_t)s * kEnc;
+  float* h1_row = st.h1 + (size_t)s * kHid;
+  float* cin_row = st.cin + (size_t)s * kCIn;
+  float* g1_row = st.g1 + (size_t)s * kHid;
+  float* g2_row = st.g2 + (size_t)s * kHid;
+  float* dh1_row = st.dh1 + (size_t)s * kHid;
+  float* dout_row = st.dout + (size_t)s * kDOut;
+  float* dg1_row = st.dg1 + (size_t)s * kHid;
+  float* dg2_row = st.dg2 + (size_t)s * kHid;
+  float* dlog_row = st.dlog + (size_t)s * 4;
+  // ---- forward recompute; activations to the staging rows ----
+  float enc[kEnc];
+  encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
+  for (int k = 0; k < kEnc; ++k) enc_row[k] = enc[k];
+  float out[kDOut];
+  for (int m = 0; m < kDOut; ++m) out[m] = 0.0f;
+  for (int j = 0; j < kHid; ++j) {
+    const float a = fmaxf(dot32(W.dw1 + j * kEnc, enc), 0.0f);
+    h1_row[j] = a;
+    for (int m = 0; m < kDOut; ++m) out[m] = fmaf(W.dw2t[j * kDOut + m], a, out[m]);
+  }
+  const float sigma = expf(out[0] - 1.0f);
+  float cin[kCIn];
+  sh16(make_float3(r.dx, r.dy, r.dz), cin);
+  for (int k = 0; k < 15; ++k) cin[16 + k] = out[1 + k];
+  cin[31] = 0.0f;
+  for (int k = 0; k < kCIn; ++k) cin_row[k] = cin[k];
+  for (int j = 0; j < kHid; ++j) g1_row[j] = fmaxf(dot32(W.cw1 + j * kCIn, cin), 0.0f);
+  float lg[3] = {0.0f, 0.0f, 0.0f};
+  for (int j = 0; j < kHid; ++j) {
+    float a = 0.0f;
+    for (int k = 0; k < kHid; ++k) a = fmaf(W.cw2[j * kHid + k], g1_row[k], a);
+    a = fmaxf(a, 0.0f);
+    g2_row[j] = a;
+    lg[0] = fmaf(W.cw3t[j * 4 + 0], a, lg[0]);
+    lg[1] = fmaf(W.cw3t[j * 4 + 1], a, lg[1]);
+    lg[2] = fmaf(W.cw3t[j * 4 + 2], a, lg[2]);
+  }
+  // ---- backward ----
+  const float c0 = sigmoidf(lg[0]), c1 = sigmoidf(lg[1]), c2 = sigmoidf(lg[2]);
+  const float dl[3] = {q.dcr * c0 * (1.0f - c0), q.dcg * c1 * (1.0f - c1), q.dcb * c2 * (1.0f - c2)};
+  dlog_row[0] = dl[0];
+  dlog_row[1] = dl[1];
+  dlog_row[2] = dl[2];
+  dlog_row[3] = 0.0f;
+  for (int j = 0; j < kHid; ++j) {
+    const float g = W.cw3t[j * 4 + 0] * dl[0] + W.cw3t[j * 4 + 1] * dl[1] + W.cw3t[j * 4 + 2] * dl[2];
+    dg2_row[j] = relu_d(g2_row[j], g);
+  }
+  for (int k = 0; k < kHid; ++k) {
+    float g = 0.0f;
+    for (int j = 0; j < kHid; ++j) g = fmaf(W.cw2[j * kHid + k], dg2_row[j], g);
+    dg1_row[k] = relu_d(g1_row[k], g);
+  }
+  float dout[kDOut];
+  dout[0] = q.dsigma * sigma;
+  for (int k = 16; k < 31; ++k) {
+    float g = 0.0f;
+    for (int j = 0; j < kHid; ++j) g = fmaf(W.cw1[j * kCIn + k], dg1_row[j], g);
+    dout[k - 15] = g;
+  }
+  for (int m = 0; m < kDOut; ++m) dout_row[m] = dout[m];
+  float denc[kEnc];
+  for (int k = 0; k < kEnc; ++k) denc[k] = 0.0f;
+  for (int j = 0; j < kHid; ++j) {
+    float g = 0.0f;
+    for (int m = 0; m < kDOut; ++m) g = fmaf(W.dw2t[j * kDOut + m], dout[m], g);
+    g = relu_d(h1_row[j], g);
+    dh1_row[j] = g;
+    for (int k = 0; k < kEnc; ++k) denc[k] = fmaf(W.dw1[j * kEnc + k], g, denc[k]);
+  }
+  // ---- hash-grid scatter-add: dtable[level][corner] += w_corner * denc[level] ----
+#pragma unroll
+  for (int l = 0; l < kLevels; ++l) {
+    const int N = level_res(l);
+    const LevelCell c = level_cell(x, N);
+    uint32_t idx[8];
+    corner_indices(c, N, (sc.dense_mask >> l) & 1u, sc.T, idx);
+    float w[8];
+    corner_weights(c, w);
+    float2* g = gtable + (size_t)l * sc.T;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) atomicAdd(g + idx[k], make_float2(w[k] * denc[2 * l], w[k] * denc[2 * l + 1]));
+  }
+}
+
+// dW[o][i] += sum_s delta[s][o] * act[s][i] over S samples (row-major rows
+// of IN activations and LDD deltas, OUT <= LDD real outputs).  Every thread
+// owns a 4x4 tile of dW; when the tiles number fewer than the block's
+// threads, the thread groups split each 32-sample smem tile between them.
+// Each block reduces a contiguous range of samples and adds its partial dW
+// with one atomic per element.
+constexpr int kDwThreads = 256;
+constexpr int kDwTile = 32;
+
+template <int IN, int OUT, int LDD>
+__global__ void __launch_bounds__(kDwThreads)
+dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32_t S, float* __restrict__ dw) {
+  static_assert(IN % 4 == 0 && LDD % 4 == 0 && OUT <= LDD, "tile shape");
+  constexpr int TI = IN / 4, TO = LDD / 4, TILES = TI * TO;
+  static_assert(TILES <= kDwThreads && kDwThreads % TILES == 0, "tile count");
+  constexpr int G = kDwThreads / TILES;  // sample groups
+  __shared__ float4 sa[kDwTile][TI];
+  __shared__ float4 sd[kDwTile][TO];
+  const int tid = threadIdx.x;
+  const int ti = tid % TI, to = (tid / TI) % TO, grp = tid / TILES;
+  float acc[4][4] = {};
+  const uint32_t per = ((S + gridDim.x - 1) / gridDim.x + kDwTile - 1) / kDwTile * kDwTile;
+  const uint32_t lo = blockIdx.x * per, hi = min(S, lo + per);
+  for (uint32_t base = lo; base < hi; base += kDwTile) {
+    const uint32_t rows = min((uint32_t)kDwTile, hi - base);
+    for (int e = tid; e < kDwTile * TI; e += kDwThreads) {
+      const int r = e / TI, c = e % TI;
+      sa[r][c] = (uint32_t)r < rows ? reinterpret_cast<const float4*>(act + (size_t)(base + r) * IN)[c]
+                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    for (int e = tid; e < kDwTile * TO; e += kDwThreads) {
+      const int r = e / TO, c = e % TO;
+      sd[r][c] = (uint32_t)r < rows ? reinterpret_cast<const float4*>(delta + (size_t)(base + r) * LDD)[c]
+                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int r = grp; r < kDwTile; r += G) {
+      const float4 a = sa[r][ti], d = sd[r][to];
+      const float av[4] = {a.x, a.y, a.z, a.w}, dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(dv[p], av[q], acc[p][q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int o = to * 4 + p;
+    if (o < OUT)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (acc[p][q] != 0.0f) atomicAdd(dw + o * IN + ti * 4 + q, acc[p][q]);
+  }
+}
+
+__global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                            size_t n, float lr, float b1, float b2, float eps, float bc1, float bc2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    g[i] = 0.0f;
+  }
+}
+
+// ---------------- FP64 loss (finite differences) ----------------
+
+struct ParamsF64 {
+  const float* table;  // FP32 table, read as double
+  const float* w;      // FP32 weight blob
+  int which;           // perturbed array: 0 table, 1 weights
+  uint64_t index;
+  double delta;
+};
+
+__device__ __forceinline__ double tab(const ParamsF64& P, uint64_t i) {
+  return (double)P.table[i] + ((P.which == 0 && i == P.index) ? P.delta : 0.0);
+}
+__device__ __forceinline__ double wt(const ParamsF64& P, int i) {
+  return (double)P.w[i] + ((P.which == 1 && (uint64_t)i == P.index) ? P.delta : 0.0);
+}
+
+// Field query in FP64: same cells and hash indices as encode_fp32 (the cell
+// is chosen from the FP32 position), FP64 weights and MLPs.
+__device__ void query_f64(const ParamsF64& P, const DevScene& sc, const float3 xf, const float3 d, double& sigma,
+                          double rgb[3]) {
+  double enc[kEnc];
+  const double x[3] = {xf.x, xf.y, xf.z};
+  for (int l = 0; l < kLevels; ++l) {
+    const int N = level_res(l);
+    const LevelCell c = level_cell(xf, N);
+    uint32_t idx[8];
+    corner_indices(c, N, (sc.dense_mask >> l) & 1u, sc.T, idx);
+    const double f[3] = {x[0] * N - (double)c.ix, x[1] * N - (double)c.iy, x[2] * N - (double)c.iz};
+    double a0 = 0, a1 = 0;
+    for (int k = 0; k < 8; ++k) {
+      const double w = ((k & 1) ? f[0] : 1 - f[0]) * ((k & 2) ? f[1] : 1 - f[1]) * ((k & 4) ? f[2] : 1 - f[2]);
+      const uint64_t e = ((uint64_t)l * sc.T + idx[k]) * 2;
+      a0 += w * tab(P, e);
+      a1 += w * tab(P, e + 1);
+    }
+    enc[2 * l] = a0;
+    enc[2 * l + 1] = a1;
+  }
+  double h1[kHid], out[kDOut];
+  for (int j = 0; j < kHid; ++j) {
+    double a = 0;
+    for (int k = 0; k < kEnc; ++k) a += wt(P, kOffDW1 + j * kEnc + k) * enc[k];
+    h1[j] = a > 0 ? a : 0;
+  }
+  for (int m = 0; m < kDOut; ++m) {
+    double a = 0;
+    for (int j = 0; j < kHid; ++j) a += wt(P, kOffDW2 + m * kHid + j) * h1[j];
+    out[m] = a;
+  }
+  sigma = exp(out[0] - 1);
+  float sh[16];
+  sh16(d, sh);  // the direction basis as rendered (FP32): it holds no parameter
+  double cin[kCIn];
+  for (int k = 0; k < 16; ++k) cin[k] = sh[k];
+  for (int k = 0; k < 15; ++k) cin[16 + k] = out[1 + k];
+  cin[31] = 0;
+  double g1[kHid];
+  for (int j = 0; j < kHid; ++j) {
+    double a = 0;
+    for (int k = 0; k < kCIn; ++k) a += wt(P, kOffCW1 + j * kCIn + k) * cin[k];
+    g1[j] = a > 0 ? a : 0;
+  }
+  double lg[3] = {0, 0, 0};
+  for (int j = 0; j < kHid; ++j) {
+    double a = 0;
+    for (int k = 0; k < kHid; ++k) a += wt(P, kOffCW2 + j * kHid + k) * g1[k];
+    a = a > 0 ? a : 0;
+    for (int c = 0; c < 3; ++c) lg[c] += wt(P, kOffCW3 + c * kHid + j) * a;
+  }
+  for (int c = 0; c < 3; ++c) rgb[c] = 1 / (1 + exp(-lg[c]));
+}
+
+// The FP32 forward's sample set (same t, positions and occupancy decisions),
+// everything downstream in FP64.
+__global__ void loss_f64_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, ParamsF64 P,
+                                double* __restrict__ loss_sum, double depth_w, double inv_n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const TrainRay r = rays[i];
+  double C[3] = {0, 0, 0}, D = 0, T = 1;
+  const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
+  for (int s = 0; s < r.n; ++s) {
+    const float t = fmaf((float)s + 0.5f, kDt, r.ts);
+    const float3 x = sample_pos(o, d, t);
+    if (!occupied(sc.occ, x)) continue;
+    double sigma, c[3];
+    query_f64(P, sc, x, d, sigma, c);
+    const double alpha = -expm1(-sigma * (double)kDt);
+    const double w = T * alpha;
+    for (int a = 0; a < 3; ++a) C[a] += w * c[a];
+    D += w * (double)t;
+    T -= w;
+    if (T < (double)kTStop) break;
+  }
+  const double e0 = C[0] - r.tr, e1 = C[1] - r.tg, e2 = C[2] - r.tb, ed = D - r.td;
+  atomicAdd(loss_sum, (e0 * e0 + e1 * e1 + e2 * e2 + depth_w * ed * ed) * inv_n);
+}
+
+}  // namespace
+
+struct nes_trainer {
+  nes_ctx* ctx = nullptr;
+  nes_train_config cfg{};
+  cudaStream_t st = nullptr;
+  TrainView* d_views = nullptr;
+  int nviews = 0;
+  const float* trgb = nullptr;
+  const float* tdep = nullptr;
+  uint32_t max_rays = 0;
+  int2* d_pairs = nullptr;
+  TrainRay* d_rays = nullptr;
+  ScratchSample* d_scratch = nullptr;  // max_rays * kMaxSteps
+  SampleRec* d_recs = nullptr;
+  uint32_t rec_capacity = 0;
+  uint32_t* d_ctr = nullptr;  // [0] record cursor, [1] error word
+  double* d_loss = nullptr;
+  float2* d_gtable = nullptr;
+  float* d_gw = nullptr;
+  float *d_mt = nullptr, *d_vt = nullptr, *d_mw = nullptr, *d_vw = nullptr;
+  float* d_stage = nullptr;
+  uint32_t chunk = 0;
+  uint64_t steps = 0;
+  uint64_t last_samples = 0;
+  // Phase events on the trainer's stream: 0 forward start, 1 forward end,
+  // 2 backward + weight-gradient end, 3 Adam start, 4 Adam end.
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  float phase_ms[3] = {0.0f, 0.0f, 0.0f};
+};
+
+namespace {
+
+#define TR_CUDA(call)                      \
+  do {                                     \
+    cudaError_t e_ = (call);               \
+    if (e_ != cudaSuccess) return NES_EIO; \
+  } while (0)
+
+constexpr int kSmemW = (int)sizeof(SmemWeights32);
+
+Staging staging(const nes_trainer* t) {
+  Staging s;
+  float* p = t->d_stage;
+  const size_t S = t->chunk;
+  s.enc = p; p += S * kEnc;
+  s.h1 = p; p += S * kHid;
+  s.cin = p; p += S * kCIn;
+  s.g1 = p; p += S * kHid;
+  s.g2 = p; p += S * kHid;
+  s.dh1 = p; p += S * kHid;
+  s.dout = p; p += S * kDOut;
+  s.dg1 = p; p += S * kHid;
+  s.dg2 = p; p += S * kHid;
+  s.dlog = p;
+  return s;
+}
+
+template <int IN, int OUT, int LDD>
+cudaError_t launch_dw(const float* act, const float* delta, uint32_t S, float* dw, int num_sms, cudaStream_t st) {
+  const uint32_t tiles = (S + kDwTile - 1) / kDwTile;
+  const uint32_t want = 2u * (uint32_t)num_sms;
+  dw_kernel<IN, OUT, LDD><<<tiles < want ? tiles : want, kDwThreads, 0, st>>>(act, delta, S, dw);
+  return cudaGetLastError();
+}
+
+// Loss and gradients (accumulated into d_gtable / d_gw) for the n rays in d_rays.
+int loss_and_grad(nes_trainer* t, int n, double* loss) {
+  nes_ctx* c = t->ctx;
+  TR_CUDA(cudaMemsetAsync(t->d_loss, 0, sizeof(double), t->st));
+  TR_CUDA(cudaMemsetAsync(t->d_ctr, 0, sizeof(uint32_t), t->st));  // the error word is cleared by the caller
+  TR_CUDA(cudaEventRecord(t->ev[0], t->st));
+  forward_kernel<<<(n + kThreads - 1) / kThreads, kThreads, kSmemW, t->st>>>(
+      t->d_rays, n, c->scene, t->d_scratch, t->d_recs, t->rec_capacity, t->d_ctr, t->d_ctr + 1, t->d_loss,
+      t->cfg.depth_weight, 1.0f / (float)n);
+  TR_CUDA(cudaGetLastError());
+  TR_CUDA(cudaEventRecord(t->ev[1], t->st));
+  uint32_t h[2] = {0, 0};
+  TR_CUDA(cudaMemcpyAsync(h, t->d_ctr, sizeof(h), cudaMemcpyDeviceToHost, t->st));
+  TR_CUDA(cudaMemcpyAsync(loss, t->d_loss, sizeof(double), cudaMemcpyDeviceToHost, t->st));
+  TR_CUDA(cudaStreamSynchronize(t->st));
+  if (h[1] == kErrOverflow) return NES_ENOMEM;
+  if (h[1]) return NES_EINVAL;
+  const uint32_t total = h[0];
+  t->last_samples = total;
+  const Staging sg = staging(t);
+  float* gw = t->d_gw;
+  const int sms = c->num_sms;
+  for (uint32_t first = 0; first < total; first += t->chunk) {
+    const uint32_t cnt = total - first < t->chunk ? total - first : t->chunk;
+    backward_kernel<<<(cnt + kThreads - 1) / kThreads, kThreads, kSmemW, t->st>>>(t->d_recs, first, cnt, t->d_rays,
+                                                                                  c->scene, sg, t->d_gtable);
+    TR_CUDA(cudaGetLastError());
+    TR_CUDA((launch_dw<kEnc, kHid, kHid>(sg.enc, sg.dh1, cnt, gw + kOffDW1, sms, t->st)));
+    TR_CUDA((launch_dw<kHid, kDOut, kDOut>(sg.h1, sg.dout, cnt, gw + kOffDW2, sms, t->st)));
+    TR_CUDA((launch_dw<kCIn, kHid, kHid>(sg.cin, sg.dg1, cnt, gw + kOffCW1, sms, t->st)));
+    TR_CUDA((launch_dw<kHid, kHid, kHid>(sg.g1, sg.dg2, cnt, gw + kOffCW2, sms, t->st)));
+    TR_CUDA((launch_dw<kHid, 3, 4>(sg.g2, sg.dlog, cnt, gw + kOffCW3, sms, t->st)));
+  }
+  TR_CUDA(cudaEventRecord(t->ev[2], t->st));
+  return NES_OK;
+}
+
+int upload_rays(nes_trainer* t, const int32_t* rays, int n) {
+  if (!rays || n < 1 || (uint32_t)n > t->max_rays || t->nviews == 0) return NES_EINVAL;
+  TR_CUDA(cudaMemsetAsync(t->d_ctr + 1, 0, sizeof(uint32_t), t->st));
+  TR_CUDA(cudaMemcpyAsync(t->d_pairs, rays, (size_t)n * sizeof(int2), cudaMemcpyHostToDevice, t->st));
+  make_rays_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(t->d_pairs, n, t->d_views, t->nviews, t->trgb, t->tdep,
+                                                       t->d_rays, t->d_ctr + 1);
+  TR_CUDA(cudaGetLastError());
+  return NES_OK;
+}
+
+int adam(nes_trainer* t) {
+  nes_ctx* c = t->ctx;
+  t->steps++;
+  const float b1 = t->cfg.beta1, b2 = t->cfg.beta2;
+  const float bc1 = (float)(1.0 - std::pow((double)b1, (double)t->steps));
+  const float bc2 = (float)(1.0 - std::pow((double)b2, (double)t->steps));
+  const size_t nt = (size_t)kLevels * c->scene.T * 2;
+  TR_CUDA(cudaEventRecord(t->ev[3], t->st));
+  adam_kernel<<<4 * c->num_sms, 256, 0, t->st>>>(reinterpret_cast<float*>(c->d_table32),
+                                                 reinterpret_cast<float*>(t->d_gtable), t->d_mt, t->d_vt, nt,
+                                                 t->cfg.lr, b1, b2, t->cfg.eps, bc1, bc2);
+  TR_CUDA(cudaGetLastError());
+  adam_kernel<<<(kWeightFloats + 255) / 256, 256, 0, t->st>>>(c->d_weights, t->d_gw, t->d_mw, t->d_vw,
+                                                              (size_t)kWeightFloats, t->cfg.lr, b1, b2, t->cfg.eps,
+                                                              bc1, bc2);
+  TR_CUDA(cudaGetLastError());
+  TR_CUDA(cudaEventRecord(t->ev[4], t->st));
+  TR_CUDA(cudaStreamSynchronize(t->st));
+  TR_CUDA(cudaEventElapsedTime(&t->phase_ms[0], t->ev[0], t->ev[1]));
+  TR_CUDA(cudaEventElapsedTime(&t->phase_ms[1], t->ev[1], t->ev[2]));
+  TR_CUDA(cudaEventElapsedTime(&t->phase_ms[2], t->ev[3], t->ev[4]));
+  return NES_OK;
+}
+
+void free_trainer(nes_trainer* t) {
+  cudaFree(t->d_views);
+  cudaFree(t->d_pairs);
+  cudaFree(t->d_rays);
+  cudaFree(t->d_scratch);
+  cudaFree(t->d_recs);
+  cudaFree(t->d_ctr);
+  cudaFree(t->d_loss);
+  cudaFree(t->d_gtable);
+  cudaFree(t->d_gw);
+  cudaFree(t->d_mt);
+  cudaFree(t->d_vt);
+  cudaFree(t->d_mw);
+  cudaFree(t->d_vw);
+  cudaFree(t->d_stage);
+  for (cudaEvent_t e : t->ev)
+    if (e) cudaEventDestroy(e);
+  if (t->st) cudaStreamDestroy(t->st);
+  delete t;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nes_train_config_default(nes_train_config* cfg) {
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->batch_rays = 1u << 18;
+  cfg->lr = 1e-2f;
+  cfg->beta1 = 0.9f;
+  cfg->beta2 = 0.99f;
+  cfg->eps = 1e-15f;
+  cfg->depth_weight = 0.1f;
+}
+
+int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** out) {
+  if (!ctx || !cfg || !out) return NES_EINVAL;
+  *out = nullptr;
+  if (ctx->cfg.precision != NES_PREC_FP32) return NES_EINVAL;
+  if (cfg->batch_rays == 0 || cfg->batch_rays > (1u << 20) || !(cfg->lr > 0.0f) || !(cfg->beta1 >= 0.0f) ||
+      !(cfg->beta1 < 1.0f) || !(cfg->beta2 >= 0.0f) || !(cfg->beta2 < 1.0f) || !(cfg->eps >= 0.0f) ||
+      !(cfg->depth_weight >= 0.0f))
+    return NES_EINVAL;
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return NES_ENODEV;
+  nes_trainer* t = new (std::nothrow) nes_trainer;
+  if (!t) return NES_ENOMEM;
+  t->ctx = ctx;
+  t->cfg = *cfg;
+  t->max_rays = cfg->batch_rays;
+  auto fail = [&](int code) {
+    free_trainer(t);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking) != cudaSuccess) return fail(NES_EIO);
+  for (cudaEvent_t& e : t->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(NES_EIO);
+  const size_t nt = (size_t)kLevels * ctx->scene.T * 2;
+  const size_t max_samples = (size_t)t->max_rays * kMaxSteps;  // every step of every ray: never overflows
+  t->rec_capacity = (uint32_t)max_samples;
+  t->chunk = 1u << 21;
+  if (cudaMalloc(&t->d_pairs, (size_t)t->max_rays * sizeof(int2)) != cudaSuccess ||
+      cudaMalloc(&t->d_rays, (size_t)t->max_rays * sizeof(TrainRay)) != cudaSuccess ||
+      cudaMalloc(&t->d_scratch, max_samples * sizeof(ScratchSample)) != cudaSuccess ||
+      cudaMalloc(&t->d_recs, max_samples * sizeof(SampleRec)) != cudaSuccess ||
+      cudaMalloc(&t->d_ctr, 2 * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&t->d_loss, sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&t->d_gtable, nt * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&t->d_gw, kWeightFloats * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&t->d_mt, nt * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&t->d_vt, nt * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&t->d_mw, kWeightFloats * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&t->d_vw, kWeightFloats * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&t->d_stage, (size_t)t->chunk * kStageFloats * sizeof(float)) != cudaSuccess)
+    return fail(NES_ENOMEM);
+  if (cudaMemset(t->d_gtable, 0, nt * sizeof(float)) != cudaSuccess ||
+      cudaMemset(t->d_gw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
+      cudaMemset(t->d_mt, 0, nt * sizeof(float)) != cudaSuccess ||
+      cudaMemset(t->d_vt, 0, nt * sizeof(float)) != cudaSuccess ||
+      cudaMemset(t->d_mw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
+      cudaMemset(t->d_vw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
+      cudaMemset(t->d_ctr, 0, 2 * sizeof(uint32_t)) != cudaSuccess)
+    return fail(NES_EIO);
+  if (cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess ||
+      cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess)
+    return fail(NES_EIO);
+  *out = t;
+  return NES_OK;
+}
+
+void nes_trainer_destroy(nes_trainer* t) {
+  if (!t) return;
+  cudaSetDevice(t->ctx->cfg.device);
+  cudaStreamSynchronize(t->st);
+  free_trainer(t);
+}
+
+int nes_trainer_set_targets(nes_trainer* t, const nes_view* views, int nviews, const float* rgb_dev,
+                            const float* depth_dev) {
+  if (!t || !views || nviews < 1 || nviews > 1024 || !rgb_dev || !depth_dev) return NES_EINVAL;
+  std::lock_guard<std::mutex> lk(t->ctx->mu);  // no render of the context meanwhile
+  TR_CUDA(cudaSetDevice(t->ctx->cfg.device));
+  std::vector<TrainView> hv(nviews);
+  uint64_t off = 0;
+  for (int i = 0; i < nviews; ++i) {
+    const uint64_t px = (uint64_t)views[i].width * views[i].height;
+    if (px == 0 || px > 0x7fffffffull || !(views[i].focal_px > 0.0f)) return NES_EINVAL;
+    std::memcpy(hv[i].M, views[i].matrix, sizeof(hv[i].M));
+    hv[i].W = (int)views[i].width;
+    hv[i].H = (int)views[i].height;
+    hv[i].focal = views[i].focal_px;
+    hv[i].pad = 0;
+    hv[i].offset = off;
+    off += px;
+  }
+  TrainView* dv = nullptr;
+  TR_CUDA(cudaMalloc(&dv, nviews * sizeof(TrainView)));
+  if (cudaMemcpy(dv, hv.data(), nviews * sizeof(TrainView), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(dv);
+    return NES_EIO;
+  }
+  cudaFree(t->d_views);
+  t->d_views = dv;
+  t->nviews = nviews;
+  t->trgb = rgb_dev;
+  t->tdep = depth_dev;
+  return NES_OK;
+}
+
+int nes_trainer_step(nes_trainer* t, uint64_t seed, double* loss) {
+  if (!t || !loss || t->nviews == 0) return NES_EINVAL;
+  std::lock_guard<std::mutex> lk(t->ctx->mu);  // no render of the context meanwhile
+  TR_CUDA(cudaSetDevice(t->ctx->cfg.device));
+  const int n = (int)t->cfg.batch_rays;
+  TR_CUDA(cudaMemsetAsync(t->d_ctr + 1, 0, sizeof(uint32_t), t->st));
+  sample_pairs_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(seed, n, t->d_views, t->nviews, t->d_pairs);
+  TR_CUDA(cudaGetLastError());
+  make_rays_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(t->d_pairs, n, t->d_views, t->nviews, t->trgb, t->tdep,
+                                                       t->d_rays, t->d_ctr + 1);
+  TR_CUDA(cudaGetLastError());
+  const int rc = loss_and_grad(t, n, loss);
+  if (rc != NES_OK) return rc;
+  return adam(t);
+}
+
+int nes_trainer_step_rays(nes_trainer* t, const int32_t* rays, int n, double* loss) {
+  if (!t || !loss) return NES_EINVAL;
+  std::lock_guard<std::mutex> lk(t->ctx->mu);  // no render of the context meanwhile
+  TR_CUDA(cudaSetDevice(t->ctx->cfg.device));
+  int rc = upload_rays(t, rays, n);
+  if (rc != NES_OK) return rc;
+  if ((rc = loss_and_grad(t, n, loss)) != NES_OK) return rc;
+  return adam(t);
+}
+
+int nes_trainer_grad(nes_trainer* t, const int32_t* rays, int n, double* loss, float* grad_table,
+                     float* grad_weights) {
+  if (!t || !loss) return NES_EINVAL;
+  std::lock_guard<std::mutex> lk(t->ctx->mu);  // no render of the context meanwhile
+  TR_CUDA(cudaSetDevice(t->ctx->cfg.device));
+  int rc = upload_rays(t, rays, n);
+  if (rc == NES_OK) rc = loss_and_grad(t, n, loss);
+  const size_t nt = (size_t)kLevels * t->ctx->scene.T * 2;
+  if (rc == NES_OK && grad_table)
+    TR_CUDA(cudaMemcpyAsync(grad_table, t->d_gtable, nt * sizeof(float), cudaMemcpyDeviceToHost, t->st));
+  if (rc == NES_OK && grad_weights)
+    TR_CUDA(cudaMemcpyAsync(grad_weights, t->d_gw, kWeightFloats * sizeof(float), cudaMemcpyDeviceToHost, t->st));
+  TR_CUDA(cudaMemsetAsync(t->d_gtable, 0, nt * sizeof(float), t->st));
+  TR_CUDA(cudaMemsetAsync(t->d_gw, 0, kWeightFloats * sizeof(float), t->st));
+  TR_CUDA(cudaStreamSynchronize(t->st));
+  return rc;
+}
+
+int nes_trainer_loss_fp64(nes_trainer* t, const int32_t* rays, int n, int which, uint64_t index, double delta,
+                          double* loss) {
+  if (!t || !loss || (which != 0 && which != 1)) return NES_EINVAL;
+  const uint64_t limit = which == 0 ? (uint64_t)kLevels * t->ctx->scene.T * 2 : (uint64_t)kWeightFloats;
+  if (index >= limit) return NES_EINVAL;
+  std::lock_guard<std::mutex> lk(t->ctx->mu);  // no render of the context meanwhile
+  TR_CUDA(cudaSetDevice(t->ctx->cfg.device));
+  int rc = upload_rays(t, rays, n);
+  if (rc != NES_OK) return rc;
+  ParamsF64 P;
+  P.table = reinterpret_cast<const float*>(t->ctx->d_table32);
+  P.w = t->ctx->d_weights;
+  P.which = which;
+  P.index = index;
+  P.delta = delta;
+  TR_CUDA(cudaMemsetAsync(t->d_loss, 0, sizeof(double), t->st));
+  loss_f64_kernel<<<(n + 63) / 64, 64, 0, t->st>>>(t->d_rays, n, t->ctx->scene, P, t->d_loss,
+                                                   (double)t->cfg.depth_weight, 1.0 / (double)n);
+  TR_CUDA(cudaGetLastError());
+  uint32_t err = 0;
+  TR_CUDA(cudaMemcpyAsync(&err, t->d_ctr + 1, sizeof(err), cudaMemcpyDeviceToHost, t->st));
+  TR_CUDA(cudaMemcpyAsync(loss, t->d_loss, sizeof(double), cudaMemcpyDeviceToHost, t->st));
+  TR_CUDA(cudaStreamSynchronize(t->st));
+  return err ? NES_EINVAL : NES_OK;
+}
+
+uint64_t nes_trainer_last_samples(const nes_trainer* t) { return t ? t->last_samples : 0; }
+
+int nes_trainer_last_timings(const nes_trainer* t, float* forward_ms, float* backward_ms, float* adam_ms) {
+  if (!t || !forward_ms || !backward_ms || !adam_ms) return NES_EINVAL;
+  if (t->steps == 0) return NES_EAGAIN;
+  *forward_ms = t->phase_ms[0];
+  *backward_ms = t->phase_ms[1];
+  *adam_ms = t->phase_ms[2];
+  return NES_OK;
+}
+
+}  // extern "C"

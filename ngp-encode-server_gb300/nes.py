@@ -88,6 +88,11 @@ class NesServerStats(ctypes.Structure):
                                                "budget_used_bytes")]
 
 
+class NesTrainConfig(ctypes.Structure):
+    _fields_ = [("batch_rays", ctypes.c_uint32), ("lr", ctypes.c_float), ("beta1", ctypes.c_float),
+                ("beta2", ctypes.c_float), ("eps", ctypes.c_float), ("depth_weight", ctypes.c_float)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _SZ = ctypes.c_size_t
@@ -128,6 +133,18 @@ _SIGS = {
     "nes_parse_frame_request": (_I, [_P, _SZ, ctypes.POINTER(NesFrameRequest)]),
     "nes_write_rendered_frame": (_I, [ctypes.POINTER(NesFrameRequest), _P, _SZ, _P, _SZ,
                                       _P, _SZ, ctypes.POINTER(_SZ)]),
+    "nes_train_config_default": (None, [ctypes.POINTER(NesTrainConfig)]),
+    "nes_trainer_create": (_I, [_P, ctypes.POINTER(NesTrainConfig), ctypes.POINTER(_P)]),
+    "nes_trainer_destroy": (None, [_P]),
+    "nes_trainer_set_targets": (_I, [_P, _P, _I, _P, _P]),
+    "nes_trainer_step": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]),
+    "nes_trainer_step_rays": (_I, [_P, _P, _I, ctypes.POINTER(ctypes.c_double)]),
+    "nes_trainer_grad": (_I, [_P, _P, _I, ctypes.POINTER(ctypes.c_double), _P, _P]),
+    "nes_trainer_loss_fp64": (_I, [_P, _P, _I, _I, ctypes.c_uint64, ctypes.c_double,
+                                   ctypes.POINTER(ctypes.c_double)]),
+    "nes_trainer_last_samples": (ctypes.c_uint64, [_P]),
+    "nes_trainer_last_timings": (_I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                      ctypes.POINTER(ctypes.c_float)]),
 }
 
 _lib = None
@@ -278,6 +295,92 @@ class Renderer:
         a, b = ctypes.c_float(0), ctypes.c_float(0)
         check(self.lib.nes_last_timings(self.h, ctypes.byref(a), ctypes.byref(b)), "nes_last_timings")
         return a.value, b.value
+
+
+class Trainer:
+    """Refits an FP32 Renderer's scene to target renders (nes_trainer_*).
+
+    Targets are device buffers (HWC FP32 RGB and FP32 depth, views
+    concatenated) that must outlive the trainer's use of them."""
+
+    def __init__(self, renderer, **kw):
+        self.lib = load()
+        self.renderer = renderer  # keeps the student context alive
+        self.cfg = NesTrainConfig()
+        self.lib.nes_train_config_default(ctypes.byref(self.cfg))
+        for k, v in kw.items():
+            setattr(self.cfg, k, v)
+        h = _P()
+        check(self.lib.nes_trainer_create(renderer.h, ctypes.byref(self.cfg), ctypes.byref(h)),
+              "nes_trainer_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.nes_trainer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_targets(self, views, rgb_ptr, depth_ptr):
+        arr = (NesView * len(views))(*views)
+        check(self.lib.nes_trainer_set_targets(self.h, arr, len(views), _P(rgb_ptr), _P(depth_ptr)),
+              "nes_trainer_set_targets")
+
+    @staticmethod
+    def _pairs(pairs):
+        import numpy as np
+        return np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+
+    def step(self, seed):
+        loss = ctypes.c_double(0)
+        check(self.lib.nes_trainer_step(self.h, seed, ctypes.byref(loss)), "nes_trainer_step")
+        return loss.value
+
+    def step_rays(self, pairs):
+        p = self._pairs(pairs)
+        loss = ctypes.c_double(0)
+        check(self.lib.nes_trainer_step_rays(self.h, p.ctypes.data, len(p), ctypes.byref(loss)),
+              "nes_trainer_step_rays")
+        return loss.value
+
+    def grad(self, pairs, table_floats):
+        """(loss, grad_table [table_floats] f32, grad_weights [9408] f32)."""
+        import numpy as np
+        p = self._pairs(pairs)
+        gt = np.empty(table_floats, np.float32)
+        gw = np.empty(9408, np.float32)
+        loss = ctypes.c_double(0)
+        check(self.lib.nes_trainer_grad(self.h, p.ctypes.data, len(p), ctypes.byref(loss), gt.ctypes.data,
+                                        gw.ctypes.data), "nes_trainer_grad")
+        return loss.value, gt, gw
+
+    def loss_fp64(self, pairs, which=0, index=0, delta=0.0):
+        p = self._pairs(pairs)
+        loss = ctypes.c_double(0)
+        check(self.lib.nes_trainer_loss_fp64(self.h, p.ctypes.data, len(p), which, index, delta,
+                                             ctypes.byref(loss)), "nes_trainer_loss_fp64")
+        return loss.value
+
+    def last_samples(self):
+        return self.lib.nes_trainer_last_samples(self.h)
+
+    def last_timings(self):
+        """(forward_ms, backward_ms, adam_ms) of the last step, CUDA events."""
+        a, b, c = ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0)
+        check(self.lib.nes_trainer_last_timings(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+              "nes_trainer_last_timings")
+        return a.value, b.value, c.value
 
 
 def rgb24_to_yuv420p(rgb_ptr, w, h, rgb_ls, y, u, v, ls, stream=0):

@@ -687,3 +687,193 @@ void oracle_overlay_text(uint8_t *rgb, int w, int h, int ls, const char *text, i
     pen_x += 12;
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* Training loss and its gradient, FP64, by reverse-mode sweeps (the    */
+/* checker of the product's nes_trainer_grad).  Per ray r of the batch  */
+/* of n: L_r = |C - C*|^2 + depth_w (D - D*)^2 with C, D from           */
+/* oracle_march_ray's compositing; L = mean of L_r.  The compositing    */
+/* adjoint runs backwards over the ray's samples carrying A = dL/dT_k:  */
+/*   g_w = dL/dw_k = g_C . c_k + g_D t_k,                               */
+/*   dL/dsigma_k = dt T_{k+1} (g_w - A_{k+1}),  dL/dc_k = g_C w_k,      */
+/*   A_k = g_w alpha_k + A_{k+1} (1 - alpha_k),  A_K = 0;               */
+/* then each sample backpropagates through both MLPs (ReLU derivative   */
+/* taken as 0 at 0) and the trilinear hash-grid lookup.                 */
+/* fp32_positions: sample t and x by the CUDA kernels' FP32 fused       */
+/* multiply-adds (t = fma(i + 1/2, dt, t_start), x = clamp(fma(t, d, o)))*/
+/* and grid cells from x*N rounded to FP32, instead of FP64, to isolate */
+/* the gradient arithmetic from the FP32 rounding of sample positions.  */
+/* g_table: 16*T*2 doubles, g_w: 9408 doubles (dw1|dw2|cw1|cw2|cw3),    */
+/* both accumulated (+=); both NULL: loss only.  Returns L.            */
+/* ------------------------------------------------------------------ */
+/* fp32_cells: the cell coordinate x*N rounded to FP32 first, as the CUDA
+ * kernels compute it (the rounding can carry x*N up to the next integer). */
+static void or_encode_corners(const or_scene *s, const double *x, int fp32_cells, double *feat,
+                              uint32_t idx[OR_LEVELS][8], double wts[OR_LEVELS][8]) {
+  for (int l = 0; l < OR_LEVELS; l++) {
+    int N = OR_RES[l];
+    double f[3];
+    uint32_t i0[3];
+    for (int a = 0; a < 3; a++) {
+      double p = fp32_cells ? (double)(float)(x[a] * (double)N) : x[a] * (double)N;
+      double fl = floor(p);
+      if (fl < 0.0) fl = 0.0;
+      if (fl > (double)(N - 1)) fl = (double)(N - 1);
+      i0[a] = (uint32_t)fl;
+      f[a] = p - fl;
+    }
+    const float *tab = s->table + (size_t)l * s->T * OR_FEATS;
+    double a0 = 0.0, a1 = 0.0;
+    for (int c = 0; c < 8; c++) {
+      int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+      wts[l][c] = (dx ? f[0] : 1.0 - f[0]) * (dy ? f[1] : 1.0 - f[1]) * (dz ? f[2] : 1.0 - f[2]);
+      idx[l][c] = oracle_grid_index((uint32_t)l, s->T, i0[0] + dx, i0[1] + dy, i0[2] + dz);
+      a0 += wts[l][c] * (double)tab[(size_t)idx[l][c] * 2 + 0];
+      a1 += wts[l][c] * (double)tab[(size_t)idx[l][c] * 2 + 1];
+    }
+    feat[2 * l] = a0;
+    feat[2 * l + 1] = a1;
+  }
+}
+
+static void or_query_cells(const or_scene *s, const double *x, const double *d, int fp32_cells,
+                           double *sigma, double *rgb) {
+  double enc[OR_ENC], h1[OR_HID], out[OR_DOUT], cin[OR_CIN], g1[OR_HID], g2[OR_HID];
+  uint32_t idx[OR_LEVELS][8];
+  double wts[OR_LEVELS][8];
+  or_encode_corners(s, x, fp32_cells, enc, idx, wts);
+  or_density(s, enc, h1, out);
+  *sigma = exp(out[0] - 1.0);
+  oracle_sh16(d, cin);
+  for (int i = 0; i < 15; i++) cin[16 + i] = out[1 + i];
+  cin[31] = 0.0;
+  or_colour(s, cin, g1, g2, rgb);
+}
+
+static void or_sample_backward(const or_scene *s, const double *x, const double *d, int fp32_cells,
+                               double dsigma, const double *dc, double *g_table, double *g_w) {
+  double enc[OR_ENC], h1[OR_HID], out[OR_DOUT], cin[OR_CIN], g1[OR_HID], g2[OR_HID], rgb[3];
+  uint32_t idx[OR_LEVELS][8];
+  double wts[OR_LEVELS][8];
+  or_encode_corners(s, x, fp32_cells, enc, idx, wts);
+  or_density(s, enc, h1, out);
+  double sigma = exp(out[0] - 1.0);
+  oracle_sh16(d, cin);
+  for (int i = 0; i < 15; i++) cin[16 + i] = out[1 + i];
+  cin[31] = 0.0;
+  or_colour(s, cin, g1, g2, rgb);
+  double *gdw1 = g_w, *gdw2 = g_w + 2048, *gcw1 = g_w + 3072, *gcw2 = g_w + 5120, *gcw3 = g_w + 9216;
+  double dl[3], dg2[OR_HID], dg1[OR_HID], dcin[OR_CIN], dout[OR_DOUT], dh1[OR_HID], denc[OR_ENC];
+  for (int c = 0; c < 3; c++) dl[c] = dc[c] * rgb[c] * (1.0 - rgb[c]);
+  for (int c = 0; c < 3; c++)
+    for (int j = 0; j < OR_HID; j++) gcw3[c * OR_HID + j] += dl[c] * g2[j];
+  for (int j = 0; j < OR_HID; j++) {
+    double a = 0.0;
+    for (int c = 0; c < 3; c++) a += (double)s->cw3[c * OR_HID + j] * dl[c];
+    dg2[j] = g2[j] > 0.0 ? a : 0.0;
+  }
+  for (int j = 0; j < OR_HID; j++)
+    for (int k = 0; k < OR_HID; k++) gcw2[j * OR_HID + k] += dg2[j] * g1[k];
+  for (int k = 0; k < OR_HID; k++) {
+    double a = 0.0;
+    for (int j = 0; j < OR_HID; j++) a += (double)s->cw2[j * OR_HID + k] * dg2[j];
+    dg1[k] = g1[k] > 0.0 ? a : 0.0;
+  }
+  for (int j = 0; j < OR_HID; j++)
+    for (int k = 0; k < OR_CIN; k++) gcw1[j * OR_CIN + k] += dg1[j] * cin[k];
+  for (int k = 0; k < OR_CIN; k++) {
+    double a = 0.0;
+    for (int j = 0; j < OR_HID; j++) a += (double)s->cw1[j * OR_CIN + k] * dg1[j];
+    dcin[k] = a;
+  }
+  dout[0] = dsigma * sigma;
+  for (int i = 0; i < 15; i++) dout[1 + i] = dcin[16 + i];
+  for (int m = 0; m < OR_DOUT; m++)
+    for (int j = 0; j < OR_HID; j++) gdw2[m * OR_HID + j] += dout[m] * h1[j];
+  for (int j = 0; j < OR_HID; j++) {
+    double a = 0.0;
+    for (int m = 0; m < OR_DOUT; m++) a += (double)s->dw2[m * OR_HID + j] * dout[m];
+    dh1[j] = h1[j] > 0.0 ? a : 0.0;
+  }
+  for (int j = 0; j < OR_HID; j++)
+    for (int k = 0; k < OR_ENC; k++) gdw1[j * OR_ENC + k] += dh1[j] * enc[k];
+  for (int k = 0; k < OR_ENC; k++) {
+    double a = 0.0;
+    for (int j = 0; j < OR_HID; j++) a += (double)s->dw1[j * OR_ENC + k] * dh1[j];
+    denc[k] = a;
+  }
+  for (int l = 0; l < OR_LEVELS; l++) {
+    double *gt = g_table + (size_t)l * s->T * OR_FEATS;
+    for (int c = 0; c < 8; c++) {
+      gt[(size_t)idx[l][c] * 2 + 0] += wts[l][c] * denc[2 * l + 0];
+      gt[(size_t)idx[l][c] * 2 + 1] += wts[l][c] * denc[2 * l + 1];
+    }
+  }
+}
+
+double oracle_train_loss_grad(const void *h, const uint32_t *occ, const float *o, const float *d,
+                              const float *ts, const int *nsteps, int n, const double *target,
+                              double depth_w, int fp32_positions, double *g_table, double *g_w) {
+  const or_scene *s = (const or_scene *)h;
+  const double dt = (double)OR_DT;
+  double loss = 0.0;
+  double *xs = (double *)malloc(sizeof(double) * OR_MAX_STEPS * 7); /* x[3], t, sigma, alpha, T_k */
+  double *cs = (double *)malloc(sizeof(double) * OR_MAX_STEPS * 3);
+  if (!xs || !cs) {
+    free(xs);
+    free(cs);
+    return NAN;
+  }
+  for (int r = 0; r < n; r++) {
+    double od[3] = {o[3 * r], o[3 * r + 1], o[3 * r + 2]}, dd[3] = {d[3 * r], d[3 * r + 1], d[3 * r + 2]};
+    double T = 1.0, C[3] = {0, 0, 0}, D = 0.0;
+    int K = 0;
+    for (int i = 0; i < nsteps[r]; i++) {
+      double t, x[3];
+      if (fp32_positions) { /* the CUDA kernels' FP32 fused multiply-adds */
+        float tf = fmaf((float)i + 0.5f, OR_DT, ts[r]);
+        t = tf;
+        for (int a = 0; a < 3; a++) {
+          float v = fmaf(tf, d[3 * r + a], o[3 * r + a]);
+          x[a] = v < 0.0f ? 0.0 : (v > 1.0f ? 1.0 : (double)v);
+        }
+      } else {
+        t = (double)ts[r] + ((double)i + 0.5) * dt;
+        for (int a = 0; a < 3; a++) {
+          double v = od[a] + t * dd[a];
+          x[a] = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
+        }
+      }
+      if (!or_occupied(occ, x)) continue;
+      double sigma, c[3];
+      or_query_cells(s, x, dd, fp32_positions, &sigma, c);
+      double alpha = -expm1(-sigma * dt);
+      double w = T * alpha;
+      double *q = xs + 7 * K;
+      q[0] = x[0]; q[1] = x[1]; q[2] = x[2]; q[3] = t; q[4] = sigma; q[5] = alpha; q[6] = T;
+      cs[3 * K] = c[0]; cs[3 * K + 1] = c[1]; cs[3 * K + 2] = c[2];
+      K++;
+      for (int a = 0; a < 3; a++) C[a] += w * c[a];
+      D += w * t;
+      T *= 1.0 - alpha;
+      if (T < OR_T_STOP) break;
+    }
+    const double *tg = target + 4 * r;
+    double e[3] = {C[0] - tg[0], C[1] - tg[1], C[2] - tg[2]}, ed = D - tg[3];
+    loss += (e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + depth_w * ed * ed) / n;
+    double gC[3] = {2.0 * e[0] / n, 2.0 * e[1] / n, 2.0 * e[2] / n}, gD = 2.0 * depth_w * ed / n;
+    double A = 0.0;
+    for (int k = K - 1; k >= 0; k--) {
+      const double *q = xs + 7 * k, *c = cs + 3 * k;
+      double alpha = q[5], Tk = q[6], w = Tk * alpha;
+      double gw = gC[0] * c[0] + gC[1] * c[1] + gC[2] * c[2] + gD * q[3];
+      double dsigma = dt * Tk * (1.0 - alpha) * (gw - A);
+      double dc[3] = {gC[0] * w, gC[1] * w, gC[2] * w};
+      if (g_table && g_w) or_sample_backward(s, q, dd, fp32_positions, dsigma, dc, g_table, g_w);
+      A = gw * alpha + A * (1.0 - alpha);
+    }
+  }
+  free(xs);
+  free(cs);
+  return loss;
+}

@@ -39,6 +39,8 @@ _SIGS = {
     "oracle_rgb_to_rgb24": (None, [_P, ctypes.c_long, _P]),
     "oracle_stream_key": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint32]),
     "oracle_overlay_text": (None, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
+    "oracle_train_loss_grad": (ctypes.c_double, [_P, _P, _P, _P, _P, _P, ctypes.c_int, _P, ctypes.c_double,
+                                                 ctypes.c_int, _P, _P]),
 }
 
 
@@ -133,6 +135,47 @@ class Scene:
         samples = self.lib.oracle_render(self.h, _ptr(occ_arr), M.ctypes.data, W, H, focal, _ptr(pixels), n,
                                          rgb.ctypes.data, depth.ctypes.data, nthreads or os.cpu_count() or 1)
         return rgb, depth, samples
+
+    def rays(self, views, pairs):
+        """FP32 ray set-up of (view, pixel) pairs; views = [(M, W, H, focal)].
+        Returns (o [n,3] f32, d [n,3] f32, ts [n] f32, nsteps [n] i32)."""
+        n = len(pairs)
+        o = np.zeros((n, 3), np.float32)
+        d = np.zeros((n, 3), np.float32)
+        ts = np.zeros(n, np.float32)
+        ns = np.zeros(n, np.int32)
+        for i, (v, p) in enumerate(pairs):
+            M, W, H, f = views[int(v)]
+            ns[i], o[i], d[i], ts[i] = ray_setup(M, W, H, f, int(p) % W, int(p) // W)
+        return o, d, ts, ns
+
+    def loss_grad(self, rays, target, depth_w=0.1, occ=None, grad=True, fp32_positions=False):
+        """Training loss (mean over rays) and its FP64 gradient.
+        rays: output of rays(); target: [n,4] (r, g, b, depth);
+        fp32_positions: sample positions rounded as the CUDA kernels round
+        them.  Returns (loss, g_table [16*T*2] f64, g_w [9408] f64) or the
+        loss alone."""
+        o, d, ts, ns = rays
+        tgt = np.ascontiguousarray(target, dtype=np.float64)
+        occ_arr = None if occ is None else np.ascontiguousarray(occ, dtype=np.uint32)
+        gt = np.zeros(16 * (1 << self.log2T) * 2, np.float64) if grad else None
+        gw = np.zeros(9408, np.float64) if grad else None
+        loss = self.lib.oracle_train_loss_grad(self.h, _ptr(occ_arr), o.ctypes.data, d.ctypes.data, ts.ctypes.data,
+                                               ns.ctypes.data, len(ns), tgt.ctypes.data, depth_w,
+                                               1 if fp32_positions else 0, _ptr(gt), _ptr(gw))
+        return (loss, gt, gw) if grad else loss
+
+    def weights_blob(self):
+        """The five weight matrices concatenated (dw1|dw2|cw1|cw2|cw3)."""
+        return np.concatenate([self.param(k) for k in range(1, 6)])
+
+    def set_weights_blob(self, blob):
+        blob = np.asarray(blob, np.float32)
+        off = 0
+        for k in range(1, 6):
+            n = self.param(k).size
+            self.set_param(k, blob[off:off + n])
+            off += n
 
 
 def ray_setup(matrix, W, H, focal, px, py):
