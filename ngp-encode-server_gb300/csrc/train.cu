@@ -70,13 +70,21 @@ struct SampleRec {  // compacted sample with its compositing adjoint
   float dsigma, dcr, dcg, dcb;
 };
 
-// Per-sample staging rows of the weight-gradient reductions.
+// Per-sample staging of the weight-gradient reductions, in 32-sample
+// tiles: feature f of sample s of an F-wide array at
+// ((s / 32) * F + f) * 32 + s % 32.  A warp's store of one feature is 128
+// contiguous bytes, a thread's features sit at small immediate offsets
+// from one base, and a tile of all F features is one contiguous block.
 constexpr int kStageFloats = kEnc + kHid + kCIn + kHid + kHid  // activations: enc, h1, cin, g1, g2
                              + kHid + kDOut + kHid + kHid + 4;  // deltas: dh1, dout, dg1, dg2, dlogit(3)+pad
 struct Staging {
-  float *enc, *h1, *cin, *g1, *g2;       // [S][32], [S][64], [S][32], [S][64], [S][64]
-  float *dh1, *dout, *dg1, *dg2, *dlog;  // [S][64], [S][16], [S][64], [S][64], [S][4]
+  float *enc, *h1, *cin, *g1, *g2;       // F = 32, 64, 32, 64, 64
+  float *dh1, *dout, *dg1, *dg2, *dlog;  // F = 64, 16, 64, 64, 4 (feature 3 unused)
 };
+
+__device__ __forceinline__ float* stage_row(float* a, int F, uint32_t s) {
+  return a + ((size_t)(s >> 5) * F) * 32 + (s & 31u);
+}
 
 constexpr int kThreads = 128;
 constexpr uint32_t kErrBadRay = 2u, kErrOverflow = 3u;
@@ -197,94 +205,175 @@ forward_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, Scra
   if ((threadIdx.x & 31u) == 0 && my_loss != 0.0f) atomicAdd(loss_sum, (double)my_loss);
 }
 
-__device__ __forceinline__ float relu_d(float a, float g) { return a > 0.0f ? g : 0.0f; }
-
 // Backward, thread per record of the chunk [first, first + count).
+// Activations stay in registers (ReLU masks as 64-bit words); every staged
+// value is written once, feature f of the sample at row[32 f].
+__device__ __forceinline__ float dot64(const float* __restrict__ w, const float in[64]) {
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+  float a = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const float4 q = w4[k];
+    a = fmaf(q.x, in[4 * k + 0], a);
+    a = fmaf(q.y, in[4 * k + 1], a);
+    a = fmaf(q.z, in[4 * k + 2], a);
+    a = fmaf(q.w, in[4 * k + 3], a);
+  }
+  return a;
+}
+
+// Shared memory of the backward: the FP32 weights plus colour W1's
+// geometry-feature columns (16..30) transposed, for the dout pass.
+struct SmemBackward {
+  SmemWeights32 w;
+  float cw1g[16 * kHid];  // [m][j] = cw1[j][16 + m], m < 15; row 15 zero
+};
+
 __global__ void __launch_bounds__(kThreads)
 backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t count, const TrainRay* __restrict__ rays,
                 const DevScene sc, Staging st, float2* __restrict__ gtable) {
   extern __shared__ float4 smem_raw[];
-  SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
+  SmemBackward& S = *reinterpret_cast<SmemBackward*>(smem_raw);
+  SmemWeights32& W = S.w;
   load_weights32(W, sc.weights);
+  for (int i = threadIdx.x; i < 16 * kHid; i += blockDim.x) {
+    const int m = i / kHid, j = i % kHid;
+    S.cw1g[i] = m < 15 ? sc.weights[kOffCW1 + j * kCIn + 16 + m] : 0.0f;
+  }
   __syncthreads();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= count) return;
   const SampleRec q = recs[first + s];
-  const TrainRay r = rays[q.ray];
   const float3 x = make_float3(q.x, q.y, q.z);
-  float* enc_row = st.enc + (size_t)s * kEnc;
-  float* h1_row = st.h1 + (size_t)s * kHid;
-  float* cin_row = st.cin + (size_t)s * kCIn;
-  float* g1_row = st.g1 + (size_t)s * kHid;
-  float* g2_row = st.g2 + (size_t)s * kHid;
-  float* dh1_row = st.dh1 + (size_t)s * kHid;
-  float* dout_row = st.dout + (size_t)s * kDOut;
-  float* dg1_row = st.dg1 + (size_t)s * kHid;
-  float* dg2_row = st.dg2 + (size_t)s * kHid;
-  float* dlog_row = st.dlog + (size_t)s * 4;
-  // ---- forward recompute; activations to the staging rows ----
+  float* const r_enc = stage_row(st.enc, kEnc, s);
+  float* const r_h1 = stage_row(st.h1, kHid, s);
+  float* const r_cin = stage_row(st.cin, kCIn, s);
+  float* const r_g1 = stage_row(st.g1, kHid, s);
+  float* const r_g2 = stage_row(st.g2, kHid, s);
+  float* const r_dh1 = stage_row(st.dh1, kHid, s);
+  float* const r_dout = stage_row(st.dout, kDOut, s);
+  float* const r_dg1 = stage_row(st.dg1, kHid, s);
+  float* const r_dg2 = stage_row(st.dg2, kHid, s);
+  float* const r_dlog = stage_row(st.dlog, 4, s);
+  // ---- forward recompute ----
   float enc[kEnc];
   encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
-  for (int k = 0; k < kEnc; ++k) enc_row[k] = enc[k];
+#pragma unroll
+  for (int k = 0; k < kEnc; ++k) r_enc[32 * k] = enc[k];
   float out[kDOut];
+#pragma unroll
   for (int m = 0; m < kDOut; ++m) out[m] = 0.0f;
+  uint64_t m_h1 = 0;
+#pragma unroll 1
   for (int j = 0; j < kHid; ++j) {
     const float a = fmaxf(dot32(W.dw1 + j * kEnc, enc), 0.0f);
-    h1_row[j] = a;
-    for (int m = 0; m < kDOut; ++m) out[m] = fmaf(W.dw2t[j * kDOut + m], a, out[m]);
+    r_h1[32 * j] = a;
+    m_h1 |= (uint64_t)(a > 0.0f) << j;
+    const float4* w2 = reinterpret_cast<const float4*>(W.dw2t + j * kDOut);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 w = w2[k];
+      out[4 * k + 0] = fmaf(w.x, a, out[4 * k + 0]);
+      out[4 * k + 1] = fmaf(w.y, a, out[4 * k + 1]);
+      out[4 * k + 2] = fmaf(w.z, a, out[4 * k + 2]);
+      out[4 * k + 3] = fmaf(w.w, a, out[4 * k + 3]);
+    }
   }
   const float sigma = expf(out[0] - 1.0f);
   float cin[kCIn];
-  sh16(make_float3(r.dx, r.dy, r.dz), cin);
+  {
+    const TrainRay& r = rays[q.ray];
+    sh16(make_float3(r.dx, r.dy, r.dz), cin);
+  }
+#pragma unroll
   for (int k = 0; k < 15; ++k) cin[16 + k] = out[1 + k];
   cin[31] = 0.0f;
-  for (int k = 0; k < kCIn; ++k) cin_row[k] = cin[k];
-  for (int j = 0; j < kHid; ++j) g1_row[j] = fmaxf(dot32(W.cw1 + j * kCIn, cin), 0.0f);
-  float lg[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < kCIn; ++k) r_cin[32 * k] = cin[k];
+  float g[kHid];  // g1, then its gradient
+#pragma unroll
   for (int j = 0; j < kHid; ++j) {
-    float a = 0.0f;
-    for (int k = 0; k < kHid; ++k) a = fmaf(W.cw2[j * kHid + k], g1_row[k], a);
-    a = fmaxf(a, 0.0f);
-    g2_row[j] = a;
-    lg[0] = fmaf(W.cw3t[j * 4 + 0], a, lg[0]);
-    lg[1] = fmaf(W.cw3t[j * 4 + 1], a, lg[1]);
-    lg[2] = fmaf(W.cw3t[j * 4 + 2], a, lg[2]);
+    g[j] = fmaxf(dot32(W.cw1 + j * kCIn, cin), 0.0f);
+    r_g1[32 * j] = g[j];
+  }
+  uint64_t m_g1 = 0;
+#pragma unroll
+  for (int j = 0; j < kHid; ++j) m_g1 |= (uint64_t)(g[j] > 0.0f) << j;
+  float lg0 = 0.0f, lg1 = 0.0f, lg2 = 0.0f;
+  uint64_t m_g2 = 0;
+#pragma unroll 1
+  for (int j = 0; j < kHid; ++j) {
+    const float a = fmaxf(dot64(W.cw2 + j * kHid, g), 0.0f);
+    r_g2[32 * j] = a;
+    m_g2 |= (uint64_t)(a > 0.0f) << j;
+    const float4 c3 = *reinterpret_cast<const float4*>(W.cw3t + j * 4);
+    lg0 = fmaf(c3.x, a, lg0);
+    lg1 = fmaf(c3.y, a, lg1);
+    lg2 = fmaf(c3.z, a, lg2);
   }
   // ---- backward ----
-  const float c0 = sigmoidf(lg[0]), c1 = sigmoidf(lg[1]), c2 = sigmoidf(lg[2]);
-  const float dl[3] = {q.dcr * c0 * (1.0f - c0), q.dcg * c1 * (1.0f - c1), q.dcb * c2 * (1.0f - c2)};
-  dlog_row[0] = dl[0];
-  dlog_row[1] = dl[1];
-  dlog_row[2] = dl[2];
-  dlog_row[3] = 0.0f;
-  for (int j = 0; j < kHid; ++j) {
-    const float g = W.cw3t[j * 4 + 0] * dl[0] + W.cw3t[j * 4 + 1] * dl[1] + W.cw3t[j * 4 + 2] * dl[2];
-    dg2_row[j] = relu_d(g2_row[j], g);
+  const float c0 = sigmoidf(lg0), c1 = sigmoidf(lg1), c2 = sigmoidf(lg2);
+  const float dl0 = q.dcr * c0 * (1.0f - c0), dl1 = q.dcg * c1 * (1.0f - c1), dl2 = q.dcb * c2 * (1.0f - c2);
+  r_dlog[0] = dl0;
+  r_dlog[32] = dl1;
+  r_dlog[64] = dl2;
+#pragma unroll
+  for (int k = 0; k < kHid; ++k) g[k] = 0.0f;
+#pragma unroll 1
+  for (int j = 0; j < kHid; ++j) {  // dg2_j, and dg1 += cw2[j][:] dg2_j
+    const float4 c3 = *reinterpret_cast<const float4*>(W.cw3t + j * 4);
+    const float d2 = ((m_g2 >> j) & 1) ? fmaf(c3.x, dl0, fmaf(c3.y, dl1, c3.z * dl2)) : 0.0f;
+    r_dg2[32 * j] = d2;
+    const float4* w4 = reinterpret_cast<const float4*>(W.cw2 + j * kHid);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const float4 w = w4[k];
+      g[4 * k + 0] = fmaf(w.x, d2, g[4 * k + 0]);
+      g[4 * k + 1] = fmaf(w.y, d2, g[4 * k + 1]);
+      g[4 * k + 2] = fmaf(w.z, d2, g[4 * k + 2]);
+      g[4 * k + 3] = fmaf(w.w, d2, g[4 * k + 3]);
+    }
   }
+#pragma unroll
   for (int k = 0; k < kHid; ++k) {
-    float g = 0.0f;
-    for (int j = 0; j < kHid; ++j) g = fmaf(W.cw2[j * kHid + k], dg2_row[j], g);
-    dg1_row[k] = relu_d(g1_row[k], g);
+    g[k] = ((m_g1 >> k) & 1) ? g[k] : 0.0f;
+    r_dg1[32 * k] = g[k];
   }
   float dout[kDOut];
   dout[0] = q.dsigma * sigma;
-  for (int k = 16; k < 31; ++k) {
-    float g = 0.0f;
-    for (int j = 0; j < kHid; ++j) g = fmaf(W.cw1[j * kCIn + k], dg1_row[j], g);
-    dout[k - 15] = g;
-  }
-  for (int m = 0; m < kDOut; ++m) dout_row[m] = dout[m];
+#pragma unroll
+  for (int m = 0; m < 15; ++m) dout[1 + m] = dot64(S.cw1g + m * kHid, g);
+#pragma unroll
+  for (int m = 0; m < kDOut; ++m) r_dout[32 * m] = dout[m];
   float denc[kEnc];
+#pragma unroll
   for (int k = 0; k < kEnc; ++k) denc[k] = 0.0f;
-  for (int j = 0; j < kHid; ++j) {
-    float g = 0.0f;
-    for (int m = 0; m < kDOut; ++m) g = fmaf(W.dw2t[j * kDOut + m], dout[m], g);
-    g = relu_d(h1_row[j], g);
-    dh1_row[j] = g;
-    for (int k = 0; k < kEnc; ++k) denc[k] = fmaf(W.dw1[j * kEnc + k], g, denc[k]);
+#pragma unroll 1
+  for (int j = 0; j < kHid; ++j) {  // dh1_j, and denc += dw1[j][:] dh1_j
+    const float4* w2 = reinterpret_cast<const float4*>(W.dw2t + j * kDOut);
+    float a = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 w = w2[k];
+      a = fmaf(w.x, dout[4 * k + 0], a);
+      a = fmaf(w.y, dout[4 * k + 1], a);
+      a = fmaf(w.z, dout[4 * k + 2], a);
+      a = fmaf(w.w, dout[4 * k + 3], a);
+    }
+    const float dh = ((m_h1 >> j) & 1) ? a : 0.0f;
+    r_dh1[32 * j] = dh;
+    const float4* w1 = reinterpret_cast<const float4*>(W.dw1 + j * kEnc);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const float4 w = w1[k];
+      denc[4 * k + 0] = fmaf(w.x, dh, denc[4 * k + 0]);
+      denc[4 * k + 1] = fmaf(w.y, dh, denc[4 * k + 1]);
+      denc[4 * k + 2] = fmaf(w.z, dh, denc[4 * k + 2]);
+      denc[4 * k + 3] = fmaf(w.w, dh, denc[4 * k + 3]);
+    }
   }
   // ---- hash-grid scatter-add: dtable[level][corner] += w_corner * denc[level] ----
-#pragma unroll
+#pragma unroll 1
   for (int l = 0; l < kLevels; ++l) {
     const int N = level_res(l);
     const LevelCell c = level_cell(x, N);
@@ -292,18 +381,24 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
     corner_indices(c, N, (sc.dense_mask >> l) & 1u, sc.T, idx);
     float w[8];
     corner_weights(c, w);
-    float2* g = gtable + (size_t)l * sc.T;
+    float2* gt = gtable + (size_t)l * sc.T;
+    float d0 = 0.0f, d1 = 0.0f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) atomicAdd(g + idx[k], make_float2(w[k] * denc[2 * l], w[k] * denc[2 * l + 1]));
+    for (int k = 0; k < kLevels; ++k)
+      if (k == l) {
+        d0 = denc[2 * k];
+        d1 = denc[2 * k + 1];
+      }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
   }
 }
 
-// dW[o][i] += sum_s delta[s][o] * act[s][i] over S samples (row-major rows
-// of IN activations and LDD deltas, OUT <= LDD real outputs).  Every thread
-// owns a 4x4 tile of dW; when the tiles number fewer than the block's
-// threads, the thread groups split each 32-sample smem tile between them.
-// Each block reduces a contiguous range of samples and adds its partial dW
-// with one atomic per element.
+// dW[o][i] += sum_s delta[s][o] * act[s][i] over S samples of tiled staging
+// (IN activation features, LDD-wide delta tiles of which OUT are real).  Every thread owns a 4x4 tile of dW; when the
+// tiles number fewer than the block's threads, the thread groups split
+// each 32-sample smem tile between them.  Each block reduces a contiguous
+// range of samples and adds its partial dW with one atomic per element.
 constexpr int kDwThreads = 256;
 constexpr int kDwTile = 32;
 
@@ -314,8 +409,10 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
   constexpr int TI = IN / 4, TO = LDD / 4, TILES = TI * TO;
   static_assert(TILES <= kDwThreads && kDwThreads % TILES == 0, "tile count");
   constexpr int G = kDwThreads / TILES;  // sample groups
-  __shared__ float4 sa[kDwTile][TI];
-  __shared__ float4 sd[kDwTile][TO];
+  // Rows padded by 4 floats: the transposing stores (sample-fastest) hit 8
+  // banks instead of 1, the float4 reads stay aligned.
+  __shared__ __align__(16) float sa[kDwTile][IN + 4];
+  __shared__ __align__(16) float sd[kDwTile][LDD + 4];
   const int tid = threadIdx.x;
   const int ti = tid % TI, to = (tid / TI) % TO, grp = tid / TILES;
   float acc[4][4] = {};
@@ -323,25 +420,26 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
   const uint32_t lo = blockIdx.x * per, hi = min(S, lo + per);
   for (uint32_t base = lo; base < hi; base += kDwTile) {
     const uint32_t rows = min((uint32_t)kDwTile, hi - base);
-    for (int e = tid; e < kDwTile * TI; e += kDwThreads) {
-      const int r = e / TI, c = e % TI;
-      sa[r][c] = (uint32_t)r < rows ? reinterpret_cast<const float4*>(act + (size_t)(base + r) * IN)[c]
-                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float* ta = act + (size_t)(base / kDwTile) * IN * kDwTile;  // contiguous tile
+    const float* td = delta + (size_t)(base / kDwTile) * LDD * kDwTile;
+    for (int e = tid; e < kDwTile * IN; e += kDwThreads) {
+      const int f = e / kDwTile, r = e % kDwTile;
+      sa[r][f] = (uint32_t)r < rows ? ta[e] : 0.0f;
     }
-    for (int e = tid; e < kDwTile * TO; e += kDwThreads) {
-      const int r = e / TO, c = e % TO;
-      sd[r][c] = (uint32_t)r < rows ? reinterpret_cast<const float4*>(delta + (size_t)(base + r) * LDD)[c]
-                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int e = tid; e < kDwTile * LDD; e += kDwThreads) {
+      const int f = e / kDwTile, r = e % kDwTile;
+      sd[r][f] = ((uint32_t)r < rows && f < OUT) ? td[e] : 0.0f;
     }
     __syncthreads();
 #pragma unroll 4
     for (int r = grp; r < kDwTile; r += G) {
-      const float4 a = sa[r][ti], d = sd[r][to];
+      const float4 a = *reinterpret_cast<const float4*>(&sa[r][ti * 4]);
+      const float4 d = *reinterpret_cast<const float4*>(&sd[r][to * 4]);
       const float av[4] = {a.x, a.y, a.z, a.w}, dv[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
       for (int p = 0; p < 4; ++p)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(dv[p], av[q], acc[p][q]);
+        for (int c = 0; c < 4; ++c) acc[p][c] = fmaf(dv[p], av[c], acc[p][c]);
     }
     __syncthreads();
   }
@@ -350,8 +448,8 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
     const int o = to * 4 + p;
     if (o < OUT)
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (acc[p][q] != 0.0f) atomicAdd(dw + o * IN + ti * 4 + q, acc[p][q]);
+      for (int c = 0; c < 4; ++c)
+        if (acc[p][c] != 0.0f) atomicAdd(dw + o * IN + ti * 4 + c, acc[p][c]);
   }
 }
 
@@ -507,6 +605,7 @@ namespace {
   } while (0)
 
 constexpr int kSmemW = (int)sizeof(SmemWeights32);
+constexpr int kSmemB = (int)sizeof(SmemBackward);
 
 Staging staging(const nes_trainer* t) {
   Staging s;
@@ -557,7 +656,7 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   const int sms = c->num_sms;
   for (uint32_t first = 0; first < total; first += t->chunk) {
     const uint32_t cnt = total - first < t->chunk ? total - first : t->chunk;
-    backward_kernel<<<(cnt + kThreads - 1) / kThreads, kThreads, kSmemW, t->st>>>(t->d_recs, first, cnt, t->d_rays,
+    backward_kernel<<<(cnt + kThreads - 1) / kThreads, kThreads, kSmemB, t->st>>>(t->d_recs, first, cnt, t->d_rays,
                                                                                   c->scene, sg, t->d_gtable);
     TR_CUDA(cudaGetLastError());
     TR_CUDA((launch_dw<kEnc, kHid, kHid>(sg.enc, sg.dh1, cnt, gw + kOffDW1, sms, t->st)));
@@ -687,7 +786,7 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaMemset(t->d_ctr, 0, 2 * sizeof(uint32_t)) != cudaSuccess)
     return fail(NES_EIO);
   if (cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess ||
-      cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess)
+      cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess)
     return fail(NES_EIO);
   *out = t;
   return NES_OK;
