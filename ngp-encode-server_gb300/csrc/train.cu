@@ -132,32 +132,66 @@ __global__ void make_rays_kernel(const int2* __restrict__ pairs, int n, const Tr
   rays[i] = r;
 }
 
-// Forward + compositing adjoint, thread per ray.  Scratch row of ray i:
-// scratch[i * kMaxSteps, +K).  Compact records: one atomic per ray.
+struct RayOut {  // composited result of one training ray
+  float C0, C1, C2, D;
+  int K;  // evaluated samples, in the ray's scratch row
+  int pad[3];
+};
+
+// Forward march, persistent: every lane marches one ray at a time and
+// claims the next ray as soon as its current one ends (one atomic per
+// warp per round of claims), so a warp never idles behind its longest ray.
+// Evaluated samples go to the ray's scratch row scratch[i * kMaxSteps, +K).
 __global__ void __launch_bounds__(kThreads)
 forward_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, ScratchSample* __restrict__ scratch,
-               SampleRec* __restrict__ recs, uint32_t capacity, uint32_t* __restrict__ cursor,
-               uint32_t* __restrict__ err, double* __restrict__ loss_sum, float depth_w, float inv_n) {
+               RayOut* __restrict__ rout, uint32_t* __restrict__ ray_cursor) {
   extern __shared__ float4 smem_raw[];
   SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
   load_weights32(W, sc.weights);
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  float my_loss = 0.0f;
-  if (i < n) {
-    const TrainRay r = rays[i];
-    ScratchSample* row = scratch + (size_t)i * kMaxSteps;
-    float C[3] = {0.0f, 0.0f, 0.0f}, D = 0.0f;
-    int K = 0;
-    const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
-    if (r.n > 0) {
-      float sh[16];
-      sh16(d, sh);
-      float T = 1.0f;
-      for (int s = 0; s < r.n; ++s) {
-        const float t = fmaf((float)s + 0.5f, kDt, r.ts);
-        const float3 x = sample_pos(o, d, t);
-        if (!occupied(sc.occ, x)) continue;
+  const unsigned lane = threadIdx.x & 31u;
+  bool live = false, exhausted = false;
+  int ray = 0, nst = 0, step = 0, K = 0;
+  float3 o = make_float3(0.0f, 0.0f, 0.0f), d = o;
+  float ts = 0.0f, T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f;
+  float sh[16];
+  ScratchSample* row = scratch;
+  for (;;) {
+    const bool want = !live && !exhausted;
+    const unsigned need = __ballot_sync(0xffffffffu, want);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(ray_cursor, (uint32_t)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (want) {
+        const uint32_t mine = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
+        if (mine < (uint32_t)n) {
+          ray = (int)mine;
+          const TrainRay r = rays[ray];
+          o = make_float3(r.ox, r.oy, r.oz);
+          d = make_float3(r.dx, r.dy, r.dz);
+          ts = r.ts;
+          nst = r.n;
+          step = 0;
+          K = 0;
+          T = 1.0f;
+          C0 = C1 = C2 = D = 0.0f;
+          sh16(d, sh);
+          row = scratch + (size_t)ray * kMaxSteps;
+          live = true;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, live)) break;
+    if (!live) continue;
+    if (step < nst) {
+      const float t = fmaf((float)step + 0.5f, kDt, ts);
+      const float3 x = sample_pos(o, d, t);
+      ++step;
+      if (occupied(sc.occ, x)) {
         float enc[kEnc];
         encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
         float dout[kDOut];
@@ -168,41 +202,73 @@ forward_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, Scra
         const float w = T * alpha;
         row[K] = ScratchSample{t, alpha, T, c.x, c.y, c.z, 0.0f, 0.0f};
         ++K;
-        C[0] = fmaf(w, c.x, C[0]);
-        C[1] = fmaf(w, c.y, C[1]);
-        C[2] = fmaf(w, c.z, C[2]);
+        C0 = fmaf(w, c.x, C0);
+        C1 = fmaf(w, c.y, C1);
+        C2 = fmaf(w, c.z, C2);
         D = fmaf(w, t, D);
         T -= w;
-        if (T < kTStop) break;
       }
     }
-    const float ec[3] = {C[0] - r.tr, C[1] - r.tg, C[2] - r.tb}, ed = D - r.td;
-    my_loss = (ec[0] * ec[0] + ec[1] * ec[1] + ec[2] * ec[2] + depth_w * ed * ed) * inv_n;
-    if (K > 0) {
-      const uint32_t base = atomicAdd(cursor, (uint32_t)K);
-      if (base + (uint32_t)K > capacity) {
-        atomicExch(err, kErrOverflow);
-      } else {
-        const float gC[3] = {2.0f * ec[0] * inv_n, 2.0f * ec[1] * inv_n, 2.0f * ec[2] * inv_n};
-        const float gD = 2.0f * depth_w * ed * inv_n;
-        float A = 0.0f;
-        for (int k = K - 1; k >= 0; --k) {
-          const ScratchSample q = row[k];
-          const float w = q.T * q.alpha;
-          const float T1 = q.T - w;
-          const float gw = fmaf(gC[0], q.cr, fmaf(gC[1], q.cg, fmaf(gC[2], q.cb, gD * q.t)));
-          const float dsig = kDt * T1 * (gw - A);
-          const float3 x = sample_pos(o, d, q.t);
-          recs[base + k] = SampleRec{x.x, x.y, x.z, (uint32_t)i, dsig, gC[0] * w, gC[1] * w, gC[2] * w};
-          A = fmaf(gw, q.alpha, A * (1.0f - q.alpha));
-        }
+    if (step >= nst || T < kTStop) {
+      rout[ray] = RayOut{C0, C1, C2, D, K, {0, 0, 0}};
+      live = false;
+    }
+  }
+}
+
+// Loss and compositing adjoint, thread per ray: the ray's samples are walked
+// backwards carrying A = dL/dT (see the file comment) and written as compact
+// records; one record-range atomic per warp (warp prefix sum of K).
+__global__ void __launch_bounds__(256)
+adjoint_kernel(const TrainRay* __restrict__ rays, const RayOut* __restrict__ rout, int n,
+               const ScratchSample* __restrict__ scratch, SampleRec* __restrict__ recs, uint32_t capacity,
+               uint32_t* __restrict__ cursor, uint32_t* __restrict__ err, double* __restrict__ loss_sum,
+               float depth_w, float inv_n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31u;
+  TrainRay r{};
+  RayOut ro{};
+  if (i < n) {
+    r = rays[i];
+    ro = rout[i];
+  }
+  const int K = i < n ? ro.K : 0;
+  int incl = K;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, off);
+    if ((int)lane >= off) incl += v;
+  }
+  uint32_t base = 0;
+  if (lane == 31 && incl > 0) base = atomicAdd(cursor, (uint32_t)incl);
+  base = __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - K);
+  float my_loss = 0.0f;
+  if (i < n) {
+    const float ec0 = ro.C0 - r.tr, ec1 = ro.C1 - r.tg, ec2 = ro.C2 - r.tb, ed = ro.D - r.td;
+    my_loss = (ec0 * ec0 + ec1 * ec1 + ec2 * ec2 + depth_w * ed * ed) * inv_n;
+    if (K > 0 && base + (uint32_t)K > capacity) {
+      atomicExch(err, kErrOverflow);
+    } else if (K > 0) {
+      const float gC0 = 2.0f * ec0 * inv_n, gC1 = 2.0f * ec1 * inv_n, gC2 = 2.0f * ec2 * inv_n;
+      const float gD = 2.0f * depth_w * ed * inv_n;
+      const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
+      const ScratchSample* row = scratch + (size_t)i * kMaxSteps;
+      float A = 0.0f;
+      for (int k = K - 1; k >= 0; --k) {
+        const ScratchSample q = row[k];
+        const float w = q.T * q.alpha;
+        const float T1 = q.T - w;
+        const float gw = fmaf(gC0, q.cr, fmaf(gC1, q.cg, fmaf(gC2, q.cb, gD * q.t)));
+        const float dsig = kDt * T1 * (gw - A);
+        const float3 x = sample_pos(o, d, q.t);
+        recs[base + k] = SampleRec{x.x, x.y, x.z, (uint32_t)i, dsig, gC0 * w, gC1 * w, gC2 * w};
+        A = fmaf(gw, q.alpha, A * (1.0f - q.alpha));
       }
     }
   }
-  // One FP64 atomic per warp.
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) my_loss += __shfl_down_sync(0xffffffffu, my_loss, off);
-  if ((threadIdx.x & 31u) == 0 && my_loss != 0.0f) atomicAdd(loss_sum, (double)my_loss);
+  if (lane == 0 && my_loss != 0.0f) atomicAdd(loss_sum, (double)my_loss);
 }
 
 // Backward, thread per record of the chunk [first, first + count).
@@ -581,13 +647,15 @@ struct nes_trainer {
   ScratchSample* d_scratch = nullptr;  // max_rays * kMaxSteps
   SampleRec* d_recs = nullptr;
   uint32_t rec_capacity = 0;
-  uint32_t* d_ctr = nullptr;  // [0] record cursor, [1] error word
+  uint32_t* d_ctr = nullptr;  // [0] record cursor, [1] error word, [2] ray cursor
+  RayOut* d_rout = nullptr;
   double* d_loss = nullptr;
   float2* d_gtable = nullptr;
   float* d_gw = nullptr;
   float *d_mt = nullptr, *d_vt = nullptr, *d_mw = nullptr, *d_vw = nullptr;
   float* d_stage = nullptr;
   uint32_t chunk = 0;
+  int fwd_blocks = 0;  // persistent forward grid: SMs x resident blocks
   uint64_t steps = 0;
   uint64_t last_samples = 0;
   // Phase events on the trainer's stream: 0 forward start, 1 forward end,
@@ -637,10 +705,14 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   nes_ctx* c = t->ctx;
   TR_CUDA(cudaMemsetAsync(t->d_loss, 0, sizeof(double), t->st));
   TR_CUDA(cudaMemsetAsync(t->d_ctr, 0, sizeof(uint32_t), t->st));  // the error word is cleared by the caller
+  TR_CUDA(cudaMemsetAsync(t->d_ctr + 2, 0, sizeof(uint32_t), t->st));
   TR_CUDA(cudaEventRecord(t->ev[0], t->st));
-  forward_kernel<<<(n + kThreads - 1) / kThreads, kThreads, kSmemW, t->st>>>(
-      t->d_rays, n, c->scene, t->d_scratch, t->d_recs, t->rec_capacity, t->d_ctr, t->d_ctr + 1, t->d_loss,
-      t->cfg.depth_weight, 1.0f / (float)n);
+  forward_kernel<<<t->fwd_blocks, kThreads, kSmemW, t->st>>>(t->d_rays, n, c->scene, t->d_scratch, t->d_rout,
+                                                             t->d_ctr + 2);
+  TR_CUDA(cudaGetLastError());
+  adjoint_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(t->d_rays, t->d_rout, n, t->d_scratch, t->d_recs,
+                                                     t->rec_capacity, t->d_ctr, t->d_ctr + 1, t->d_loss,
+                                                     t->cfg.depth_weight, 1.0f / (float)n);
   TR_CUDA(cudaGetLastError());
   TR_CUDA(cudaEventRecord(t->ev[1], t->st));
   uint32_t h[2] = {0, 0};
@@ -709,6 +781,7 @@ void free_trainer(nes_trainer* t) {
   cudaFree(t->d_rays);
   cudaFree(t->d_scratch);
   cudaFree(t->d_recs);
+  cudaFree(t->d_rout);
   cudaFree(t->d_ctr);
   cudaFree(t->d_loss);
   cudaFree(t->d_gtable);
@@ -767,7 +840,8 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaMalloc(&t->d_rays, (size_t)t->max_rays * sizeof(TrainRay)) != cudaSuccess ||
       cudaMalloc(&t->d_scratch, max_samples * sizeof(ScratchSample)) != cudaSuccess ||
       cudaMalloc(&t->d_recs, max_samples * sizeof(SampleRec)) != cudaSuccess ||
-      cudaMalloc(&t->d_ctr, 2 * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&t->d_rout, (size_t)t->max_rays * sizeof(RayOut)) != cudaSuccess ||
+      cudaMalloc(&t->d_ctr, 4 * sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc(&t->d_loss, sizeof(double)) != cudaSuccess ||
       cudaMalloc(&t->d_gtable, nt * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&t->d_gw, kWeightFloats * sizeof(float)) != cudaSuccess ||
@@ -783,11 +857,15 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaMemset(t->d_vt, 0, nt * sizeof(float)) != cudaSuccess ||
       cudaMemset(t->d_mw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
       cudaMemset(t->d_vw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
-      cudaMemset(t->d_ctr, 0, 2 * sizeof(uint32_t)) != cudaSuccess)
+      cudaMemset(t->d_ctr, 0, 4 * sizeof(uint32_t)) != cudaSuccess)
     return fail(NES_EIO);
   if (cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess ||
       cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess)
     return fail(NES_EIO);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_kernel, kThreads, kSmemW) != cudaSuccess)
+    return fail(NES_EIO);
+  t->fwd_blocks = ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
   *out = t;
   return NES_OK;
 }
