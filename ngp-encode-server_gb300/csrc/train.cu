@@ -86,7 +86,12 @@ __device__ __forceinline__ float* stage_row(float* a, int F, uint32_t s) {
   return a + ((size_t)(s >> 5) * F) * 32 + (s & 31u);
 }
 
-constexpr int kThreads = 128;
+// Forward: 128-thread blocks, three resident per SM at its 135 registers.
+// Backward: 256-thread blocks capped at 128 registers, two resident per SM
+// (16 warps) with one shared copy of the weights per block, which leaves
+// L1 for the table gathers.
+constexpr int kFwdThreads = 128;
+constexpr int kBwdThreads = 256;
 constexpr uint32_t kErrBadRay = 2u, kErrOverflow = 3u;
 
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
@@ -142,7 +147,7 @@ struct RayOut {  // composited result of one training ray
 // claims the next ray as soon as its current one ends (one atomic per
 // warp per round of claims), so a warp never idles behind its longest ray.
 // Evaluated samples go to the ray's scratch row scratch[i * kMaxSteps, +K).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kFwdThreads)
 forward_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, ScratchSample* __restrict__ scratch,
                RayOut* __restrict__ rout, uint32_t* __restrict__ ray_cursor) {
   extern __shared__ float4 smem_raw[];
@@ -295,7 +300,7 @@ struct SmemBackward {
   float cw1g[16 * kHid];  // [m][j] = cw1[j][16 + m], m < 15; row 15 zero
 };
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kBwdThreads, 2)
 backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t count, const TrainRay* __restrict__ rays,
                 const DevScene sc, Staging st, float2* __restrict__ gtable) {
   extern __shared__ float4 smem_raw[];
@@ -486,15 +491,25 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
   const uint32_t lo = blockIdx.x * per, hi = min(S, lo + per);
   for (uint32_t base = lo; base < hi; base += kDwTile) {
     const uint32_t rows = min((uint32_t)kDwTile, hi - base);
-    const float* ta = act + (size_t)(base / kDwTile) * IN * kDwTile;  // contiguous tile
-    const float* td = delta + (size_t)(base / kDwTile) * LDD * kDwTile;
-    for (int e = tid; e < kDwTile * IN; e += kDwThreads) {
-      const int f = e / kDwTile, r = e % kDwTile;
-      sa[r][f] = (uint32_t)r < rows ? ta[e] : 0.0f;
+    // The tile is one contiguous block: float4 loads of 4 samples of one
+    // feature, stored transposed.
+    const float4* ta = reinterpret_cast<const float4*>(act + (size_t)(base / kDwTile) * IN * kDwTile);
+    const float4* td = reinterpret_cast<const float4*>(delta + (size_t)(base / kDwTile) * LDD * kDwTile);
+    for (int e = tid; e < kDwTile * IN / 4; e += kDwThreads) {
+      const int f = (4 * e) / kDwTile, r = (4 * e) % kDwTile;
+      const float4 v = ta[e];
+      sa[r + 0][f] = (uint32_t)(r + 0) < rows ? v.x : 0.0f;
+      sa[r + 1][f] = (uint32_t)(r + 1) < rows ? v.y : 0.0f;
+      sa[r + 2][f] = (uint32_t)(r + 2) < rows ? v.z : 0.0f;
+      sa[r + 3][f] = (uint32_t)(r + 3) < rows ? v.w : 0.0f;
     }
-    for (int e = tid; e < kDwTile * LDD; e += kDwThreads) {
-      const int f = e / kDwTile, r = e % kDwTile;
-      sd[r][f] = ((uint32_t)r < rows && f < OUT) ? td[e] : 0.0f;
+    for (int e = tid; e < kDwTile * LDD / 4; e += kDwThreads) {
+      const int f = (4 * e) / kDwTile, r = (4 * e) % kDwTile;
+      const float4 v = f < OUT ? td[e] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      sd[r + 0][f] = (uint32_t)(r + 0) < rows ? v.x : 0.0f;
+      sd[r + 1][f] = (uint32_t)(r + 1) < rows ? v.y : 0.0f;
+      sd[r + 2][f] = (uint32_t)(r + 2) < rows ? v.z : 0.0f;
+      sd[r + 3][f] = (uint32_t)(r + 3) < rows ? v.w : 0.0f;
     }
     __syncthreads();
 #pragma unroll 4
@@ -695,7 +710,7 @@ Staging staging(const nes_trainer* t) {
 template <int IN, int OUT, int LDD>
 cudaError_t launch_dw(const float* act, const float* delta, uint32_t S, float* dw, int num_sms, cudaStream_t st) {
   const uint32_t tiles = (S + kDwTile - 1) / kDwTile;
-  const uint32_t want = 2u * (uint32_t)num_sms;
+  const uint32_t want = 8u * (uint32_t)num_sms;  // 8 resident 256-thread blocks per SM
   dw_kernel<IN, OUT, LDD><<<tiles < want ? tiles : want, kDwThreads, 0, st>>>(act, delta, S, dw);
   return cudaGetLastError();
 }
@@ -707,7 +722,7 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   TR_CUDA(cudaMemsetAsync(t->d_ctr, 0, sizeof(uint32_t), t->st));  // the error word is cleared by the caller
   TR_CUDA(cudaMemsetAsync(t->d_ctr + 2, 0, sizeof(uint32_t), t->st));
   TR_CUDA(cudaEventRecord(t->ev[0], t->st));
-  forward_kernel<<<t->fwd_blocks, kThreads, kSmemW, t->st>>>(t->d_rays, n, c->scene, t->d_scratch, t->d_rout,
+  forward_kernel<<<t->fwd_blocks, kFwdThreads, kSmemW, t->st>>>(t->d_rays, n, c->scene, t->d_scratch, t->d_rout,
                                                              t->d_ctr + 2);
   TR_CUDA(cudaGetLastError());
   adjoint_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(t->d_rays, t->d_rout, n, t->d_scratch, t->d_recs,
@@ -728,7 +743,7 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   const int sms = c->num_sms;
   for (uint32_t first = 0; first < total; first += t->chunk) {
     const uint32_t cnt = total - first < t->chunk ? total - first : t->chunk;
-    backward_kernel<<<(cnt + kThreads - 1) / kThreads, kThreads, kSmemB, t->st>>>(t->d_recs, first, cnt, t->d_rays,
+    backward_kernel<<<(cnt + kBwdThreads - 1) / kBwdThreads, kBwdThreads, kSmemB, t->st>>>(t->d_recs, first, cnt, t->d_rays,
                                                                                   c->scene, sg, t->d_gtable);
     TR_CUDA(cudaGetLastError());
     TR_CUDA((launch_dw<kEnc, kHid, kHid>(sg.enc, sg.dh1, cnt, gw + kOffDW1, sms, t->st)));
@@ -863,7 +878,7 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess)
     return fail(NES_EIO);
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_kernel, kThreads, kSmemW) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_kernel, kFwdThreads, kSmemW) != cudaSuccess)
     return fail(NES_EIO);
   t->fwd_blocks = ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
   *out = t;
