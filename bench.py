@@ -39,7 +39,7 @@ FLOP_PER_SAMPLE = 18688          # 2 x 9,344 MLP multiply-adds
 GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
 # dram__bytes_read.sum + dram__bytes_write.sum of one full 1920x1080 march
 # launch, from the ncu captures summarised in profiles/march_*_1080p.md.
-DRAM_BYTES_PER_LAUNCH = {"fp16": 48.443e6 + 1.015e6, "fp32": 73.651e6 + 7.437e6}
+DRAM_BYTES_PER_LAUNCH = {"fp16": 48.435e6 + 1.166e6, "fp32": 73.651e6 + 7.437e6}
 WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
 
 
