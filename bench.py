@@ -16,10 +16,13 @@ uint16 mm, all on the device with the scene resident.  L2 is flushed (a
           planes + packed depth copied back to pinned host buffers inside
           the timed region), plus p50/p99 pose->YUV latency.
 
---impl reference times the CPU restatement of the path (oracle/, FP64,
-all host threads) on bounded random pixel samples of the same requests: the
+--impl reference times the plain FP32 CPU render of the path (oracle/, all
+host threads) on bounded random pixel samples of the same requests: the
 reference's renderer is an external project and its swscale/libavcodec
-dependencies are not installed, so the oracle port is the CPU arm.
+dependencies are not installed, so the CPU restatement is the CPU arm.  The
+default run's cpu_baseline times the same FP32 CPU render and the FP64
+oracle (the checker) on one pixel sample, with the parity of the
+tensor-core render against the FP64 oracle on those pixels.
 """
 import argparse
 import json
@@ -55,6 +58,9 @@ def parse_args():
     p.add_argument("--no-extras", action="store_true", help="skip the stereo and serving sections")
     p.add_argument("--serve-seconds", type=float, default=2.0)
     p.add_argument("--train-steps", type=int, default=20, help="refit steps timed in the training section")
+    p.add_argument("--train-batch", type=int, default=1 << 18, help="rays per refit step")
+    p.add_argument("--section", choices=["all", "training"], default="all",
+                   help="'training' prints only the refit section (for profiling captures)")
     p.add_argument("--width", type=int, default=1920, help="smaller sizes only for profiling captures")
     p.add_argument("--height", type=int, default=1080)
     return p.parse_args()
@@ -123,8 +129,9 @@ def load_peaks():
         return 6800.0, 1900.0, 1700.0, "fallback"
 
 
-def cpu_sample(poses, steps_px, seed):
-    """Times the FP64 oracle on random pixel subsets; returns (Mrays/s, s, px, threads)."""
+def cpu_sample(poses, steps_px, seed, fp32=True):
+    """Times the CPU render (plain FP32, or the FP64 oracle) on random pixel
+    subsets; returns (Mrays/s, s, px, threads)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import numpy as np
     import nes
@@ -136,8 +143,9 @@ def cpu_sample(poses, steps_px, seed):
     total_px, total_s = 0, 0.0
     for i, npx in enumerate(steps_px):
         pix = rng.choice(W * H, npx, replace=False).astype(np.int32)
+        render = scene.render_f32 if fp32 else scene.render
         t0 = time.perf_counter()
-        scene.render(poses[i % len(poses)], W, H, f, pixels=pix, nthreads=threads)
+        render(poses[i % len(poses)], W, H, f, pixels=pix, nthreads=threads)
         total_s += time.perf_counter() - t0
         total_px += npx
     return total_px / total_s / 1e6, total_s, total_px, threads
@@ -155,12 +163,12 @@ def run_reference(args):
     line = {"metric": "Mrays/s (pose->YUV render, all pixels)", "value": round(mrays, 6), "unit": "Mrays/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene and poses)",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and poses)",
             "config": {"workload": WORKLOAD, "sample": "%d random pixels per step" % per_step,
                        "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": round(mrays, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": "%d random pixels of a 1920x1080 request per step, %d steps" % (per_step,
-                                                                                                   args.steps)},
+                             "sample": "plain FP32 CPU render (oracle/, pthreads) of %d random pixels of a "
+                                       "1920x1080 request per step, %d steps" % (per_step, args.steps)},
             "e2e": {"value": round(mrays, 6), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -298,6 +306,8 @@ def run_ours(args):
                      "kernel": "march", "peak_source": src + " bf16 sustained",
                      "march_ms": round(head["march_ms"], 3), "raygen_ms": round(head["raygen_ms"], 4),
                      "samples_per_step": int(head["samples_per_step"]),
+                     "msamples_per_s": round(head["samples_per_step"] / (head["march_ms"] / 1e3) / 1e6, 1),
+                     "frames_per_s": round(1e3 / head["ms_per_step"], 2),
                      "gather_gbs": round(head["samples_per_step"] * GATHER_BYTES[kind] / (head["march_ms"] / 1e3) / 1e9, 1)},
         "clocks": head["clocks"],
         "paths": {("fp16_tc" if k == nes.PREC_FP16_TC else "fp32"):
@@ -308,8 +318,9 @@ def run_ours(args):
     if world == 1 and not args.no_extras:
         line["stereo"] = run_stereo(dev, min(args.steps, 20))
         line["serving"] = run_serving(dev, args.serve_seconds)
+        line["glue"] = run_glue(dev, {"hbm_gbs": hbm})
         if args.train_steps > 0:
-            line["training"] = run_training(dev, args.train_steps)
+            line["training"] = run_training(dev, args.train_steps, batch=args.train_batch)
     if not args.no_cpu_baseline:
         per = (W * H) // 32
         cb = cpu_baseline_with_parity(dev, poses[0], per)
@@ -337,13 +348,18 @@ def cpu_baseline_with_parity(dev, pose, npx):
     pix = np.random.default_rng(7).choice(W * H, npx, replace=False).astype(np.int32)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
+    scene.render_f32(pose, W, H, f, pixels=pix, nthreads=threads)
+    secs32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
     orgb, odep, _ = scene.render(pose, W, H, f, pixels=pix, nthreads=threads)
     secs = time.perf_counter() - t0
     mse = float(np.mean((g_rgb[pix] - orgb) ** 2))
-    return {"value": round(npx / secs / 1e6, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": "%d random pixels of one 1920x1080 request (FP64 oracle, %.1f s)" % (npx, secs),
+    return {"value": round(npx / secs32 / 1e6, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": "%d random pixels of one 1920x1080 request, plain FP32 CPU render (%.1f s)" % (npx, secs32),
+            "fp64_oracle": {"value": round(npx / secs / 1e6, 6), "unit": "Mrays/s", "seconds": round(secs, 2)},
             "parity_fp16_tc": {"psnr_db": round(10 * math.log10(1.0 / mse), 2) if mse > 0 else None,
-                               "max_abs_depth_err": float(np.abs(g_dep[pix] - odep).max()), "pixels": npx}}
+                               "max_abs_depth_err": float(np.abs(g_dep[pix] - odep).max()), "pixels": npx,
+                               "against": "FP64 oracle"}}
 
 
 def run_stereo(dev, steps):
@@ -396,6 +412,87 @@ def run_stereo(dev, steps):
             "mrays": round(2 * SW * SH * steps / (sum(ms) / 1e3) / 1e6, 3),
             "samples_per_pixel": round(statistics.mean(samples) / (2 * SW * SH), 2),
             "timing": "CUDA events around each request (device time, pose already on the host)"}
+
+
+def run_glue(dev, peaks):
+    """Frame glue on its configured inputs: 30 frames of 1280x720 RGB24 (50/50
+    blend of U(0,255) bytes and a horizontal gradient) and FP32 depth
+    U(0.1, 10), per kernel timed with CUDA events over the 30 frames after an
+    L2 flush (a 1280x720 launch moves 4.1 MB: launch-latency bound); plus one
+    7680x4320 frame per kernel, L2 flushed, for the HBM roofline.  Frame 0 is
+    checked bit for bit against the oracle's integer restatement."""
+    import numpy as np
+    import torch
+    import nes
+    lib = nes.load()
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    hbm = peaks.get("hbm_gbs")
+
+    def frames(w, h, n, seed):
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        noise = torch.randint(0, 256, (n, h, w, 3), generator=g, device=dev, dtype=torch.int32)
+        grad = (torch.arange(w, device=dev, dtype=torch.int32) * 255 // max(1, w - 1)).view(1, 1, w, 1)
+        rgb = ((noise + grad) // 2).to(torch.uint8).reshape(n, -1)
+        dep = (torch.rand((n, h * w), generator=g, device=dev) * 9.9 + 0.1).contiguous()
+        return rgb, dep
+
+    def timed(fn, n):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for i in range(n):
+            fn(i)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / n
+
+    out = {}
+    for tag, (w, h, n) in {"1280x720_x30": (1280, 720, 30), "7680x4320": (7680, 4320, 1)}.items():
+        rgb, dep = frames(w, h, n, 5)
+        ls = nes.linesizes(w)
+        ch = (h + 1) // 2
+        ysz = ls[0] * h + 2 * ls[1] * ch
+        yuv = torch.empty((n, ysz), dtype=torch.uint8, device=dev)
+        gray = torch.empty((n, w * h), dtype=torch.uint8, device=dev)
+        dmm = torch.empty((n, w * h), dtype=torch.int16, device=dev)
+
+        def to_yuv(i, src=rgb, gray_src=False):
+            y = yuv[i].data_ptr()
+            fn = nes.gray8_to_yuv420p if gray_src else nes.rgb24_to_yuv420p
+            fn(src[i].data_ptr(), w, h, w if gray_src else 3 * w, y, y + ls[0] * h, y + ls[0] * h + ls[1] * ch,
+               ls, sptr)
+
+        for i in range(min(n, 3)):  # warm-up
+            to_yuv(i)
+        px = w * h
+        ms_rgb = timed(to_yuv, n)
+        ms_dep = timed(lambda i: nes.depth_pack_u16mm(dep[i].data_ptr(), px, dmm[i].data_ptr(), sptr), n)
+        ms_g8 = timed(lambda i: nes.check(lib.nes_depth_to_gray8(dep[i].data_ptr(), px, 4.0, gray[i].data_ptr(),
+                                                                 sptr), "gray8"), n)
+        ms_gy = timed(lambda i: to_yuv(i, gray, True), n)
+        ent = {}
+        for k, ms, bpp in (("rgb24_to_yuv420p", ms_rgb, 4.5), ("depth_pack_u16mm", ms_dep, 6.0),
+                           ("depth_to_gray8", ms_g8, 5.0), ("gray8_to_yuv420p", ms_gy, 2.5)):
+            gbs = px * bpp / (ms / 1e3) / 1e9
+            ent[k] = {"us_per_frame": round(ms * 1e3, 2), "gbs": round(gbs, 1),
+                      "frac_of_hbm": round(gbs / hbm, 3) if hbm else None, "bytes_per_px": bpp}
+        if tag.startswith("1280"):
+            sys.path.insert(0, os.path.join(REPO, "oracle"))
+            import oracle
+            torch.cuda.synchronize()
+            img = rgb[0].cpu().numpy()
+            oy, ou, ov = oracle.rgb24_to_yuv420p(img, w, h, 3 * w, ls)
+            got = yuv[0].cpu().numpy()
+            exact = (np.array_equal(got[:ls[0] * h], oy) and np.array_equal(got[ls[0] * h:ls[0] * h + ls[1] * ch], ou)
+                     and np.array_equal(got[ls[0] * h + ls[1] * ch:], ov))
+            exact_d = np.array_equal(dmm[0].cpu().numpy().view(np.uint16), oracle.depth_pack_u16mm(dep[0].cpu().numpy()))
+            ent["bit_exact_vs_oracle"] = bool(exact and exact_d)
+        out[tag] = ent
+    out["timing"] = "CUDA events over back-to-back launches after a 256 MiB L2 flush; GB/s from algorithmic bytes per pixel"
+    return out
 
 
 def run_training(dev, steps, nviews=32, side=400, batch=1 << 18):
@@ -569,6 +666,11 @@ def main():
         WORKLOAD = WORKLOAD.replace("1920x1080", "%dx%d (profiling case)" % (W, H))
     if args.impl == "reference":
         run_reference(args)
+    elif args.section == "training":
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        torch.cuda.set_device(dev)
+        print(json.dumps({"training": run_training(dev, args.train_steps, batch=args.train_batch)}), flush=True)
     else:
         run_ours(args)
 

@@ -877,3 +877,153 @@ double oracle_train_loss_grad(const void *h, const uint32_t *occ, const float *o
   free(cs);
   return loss;
 }
+
+/* ------------------------------------------------------------------ */
+/* Plain FP32 CPU render: the same scene, march and compositing in     */
+/* single precision, pthreads over host cores.  A CPU speed baseline    */
+/* (the FP32 counterpart of the GPU plain path), not a checker.         */
+/* ------------------------------------------------------------------ */
+static void or_query_f32(const or_scene *s, const float *x, const float *sh, float *sigma, float *rgb) {
+  float enc[OR_ENC], h1[OR_HID], out[OR_DOUT], cin[OR_CIN], g1[OR_HID];
+  for (int l = 0; l < OR_LEVELS; l++) {
+    int N = OR_RES[l];
+    float f[3];
+    uint32_t i0[3];
+    for (int a = 0; a < 3; a++) {
+      float p = x[a] * (float)N;
+      float fl = floorf(p);
+      if (fl < 0.0f) fl = 0.0f;
+      if (fl > (float)(N - 1)) fl = (float)(N - 1);
+      i0[a] = (uint32_t)fl;
+      f[a] = p - fl;
+    }
+    const float *tab = s->table + (size_t)l * s->T * OR_FEATS;
+    float a0 = 0.0f, a1 = 0.0f;
+    for (int c = 0; c < 8; c++) {
+      int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+      float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
+      uint32_t idx = oracle_grid_index((uint32_t)l, s->T, i0[0] + dx, i0[1] + dy, i0[2] + dz);
+      a0 += w * tab[(size_t)idx * 2];
+      a1 += w * tab[(size_t)idx * 2 + 1];
+    }
+    enc[2 * l] = a0;
+    enc[2 * l + 1] = a1;
+  }
+  for (int m = 0; m < OR_DOUT; m++) out[m] = 0.0f;
+  for (int j = 0; j < OR_HID; j++) {
+    float a = 0.0f;
+    for (int k = 0; k < OR_ENC; k++) a += s->dw1[j * OR_ENC + k] * enc[k];
+    h1[j] = a > 0.0f ? a : 0.0f;
+  }
+  for (int m = 0; m < OR_DOUT; m++) {
+    float a = 0.0f;
+    for (int j = 0; j < OR_HID; j++) a += s->dw2[m * OR_HID + j] * h1[j];
+    out[m] = a;
+  }
+  *sigma = expf(out[0] - 1.0f);
+  for (int k = 0; k < 16; k++) cin[k] = sh[k];
+  for (int k = 0; k < 15; k++) cin[16 + k] = out[1 + k];
+  cin[31] = 0.0f;
+  for (int j = 0; j < OR_HID; j++) {
+    float a = 0.0f;
+    for (int k = 0; k < OR_CIN; k++) a += s->cw1[j * OR_CIN + k] * cin[k];
+    g1[j] = a > 0.0f ? a : 0.0f;
+  }
+  float lg[3] = {0.0f, 0.0f, 0.0f};
+  for (int j = 0; j < OR_HID; j++) {
+    float a = 0.0f;
+    for (int k = 0; k < OR_HID; k++) a += s->cw2[j * OR_HID + k] * g1[k];
+    a = a > 0.0f ? a : 0.0f;
+    for (int c = 0; c < 3; c++) lg[c] += s->cw3[c * OR_HID + j] * a;
+  }
+  for (int c = 0; c < 3; c++) rgb[c] = 1.0f / (1.0f + expf(-lg[c]));
+}
+
+typedef struct {
+  const or_scene *s;
+  const uint32_t *occ;
+  const float *M;
+  int W, H;
+  float focal;
+  const int32_t *pix;
+  long npix;
+  float *rgb, *depth;
+  long next;
+  long long samples;
+  pthread_mutex_t mu;
+} or_render32_job;
+
+static void *or_render32_worker(void *arg) {
+  or_render32_job *j = (or_render32_job *)arg;
+  long long local = 0;
+  for (;;) {
+    pthread_mutex_lock(&j->mu);
+    long b = j->next;
+    j->next += 64;
+    pthread_mutex_unlock(&j->mu);
+    if (b >= j->npix) break;
+    long e = b + 64 < j->npix ? b + 64 : j->npix;
+    for (long k = b; k < e; k++) {
+      long p = j->pix ? (long)j->pix[k] : k;
+      float o[3], d[3], ts;
+      int n = oracle_ray_setup(j->M, j->W, j->H, j->focal, (int)(p % j->W), (int)(p / j->W), o, d, &ts);
+      float C[3] = {0.0f, 0.0f, 0.0f}, D = 0.0f, T = 1.0f;
+      double dd[3] = {d[0], d[1], d[2]}, shd[16];
+      float sh[16];
+      oracle_sh16(dd, shd);
+      for (int i = 0; i < 16; i++) sh[i] = (float)shd[i];
+      for (int i = 0; i < n; i++) {
+        float t = ts + ((float)i + 0.5f) * OR_DT;
+        float x[3];
+        double xd[3];
+        for (int a = 0; a < 3; a++) {
+          float v = o[a] + t * d[a];
+          x[a] = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+          xd[a] = x[a];
+        }
+        if (!or_occupied(j->occ, xd)) continue;
+        float sigma, c[3];
+        or_query_f32(j->s, x, sh, &sigma, c);
+        local++;
+        float alpha = -expm1f(-sigma * OR_DT), w = T * alpha;
+        for (int a = 0; a < 3; a++) C[a] += w * c[a];
+        D += w * t;
+        T -= w;
+        if (T < (float)OR_T_STOP) break;
+      }
+      for (int a = 0; a < 3; a++) j->rgb[k * 3 + a] = C[a];
+      j->depth[k] = D;
+    }
+  }
+  pthread_mutex_lock(&j->mu);
+  j->samples += local;
+  pthread_mutex_unlock(&j->mu);
+  return NULL;
+}
+
+/* FP32 render of the listed pixels (or all W*H); rgb npix*3, depth npix
+ * floats.  Returns the number of field evaluations. */
+long long oracle_render_f32(const void *h, const uint32_t *occ, const float *M, int W, int H, float focal,
+                            const int32_t *pix, long npix, float *rgb, float *depth, int nthreads) {
+  or_render32_job j;
+  j.s = (const or_scene *)h;
+  j.occ = occ;
+  j.M = M;
+  j.W = W;
+  j.H = H;
+  j.focal = focal;
+  j.pix = pix;
+  j.npix = pix ? npix : (long)W * H;
+  j.rgb = rgb;
+  j.depth = depth;
+  j.next = 0;
+  j.samples = 0;
+  pthread_mutex_init(&j.mu, NULL);
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, or_render32_worker, &j);
+  for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+  pthread_mutex_destroy(&j.mu);
+  return j.samples;
+}

@@ -39,6 +39,8 @@ _SIGS = {
     "oracle_rgb_to_rgb24": (None, [_P, ctypes.c_long, _P]),
     "oracle_stream_key": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint32]),
     "oracle_overlay_text": (None, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
+    "oracle_render_f32": (ctypes.c_longlong, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_float, _P,
+                                              ctypes.c_long, _P, _P, ctypes.c_int]),
     "oracle_train_loss_grad": (ctypes.c_double, [_P, _P, _P, _P, _P, _P, ctypes.c_int, _P, ctypes.c_double,
                                                  ctypes.c_int, _P, _P]),
 }
@@ -134,6 +136,22 @@ class Scene:
         occ_arr = None if occ is None else np.ascontiguousarray(occ, dtype=np.uint32)
         samples = self.lib.oracle_render(self.h, _ptr(occ_arr), M.ctypes.data, W, H, focal, _ptr(pixels), n,
                                          rgb.ctypes.data, depth.ctypes.data, nthreads or os.cpu_count() or 1)
+        return rgb, depth, samples
+
+    def render_f32(self, matrix, W, H, focal, pixels=None, occ=None, nthreads=None):
+        """Plain FP32 CPU render (a speed baseline, not the checker).
+        Returns (rgb [n,3] f32, depth [n] f32, samples)."""
+        M = np.ascontiguousarray(matrix, dtype=np.float32)
+        if pixels is not None:
+            pixels = np.ascontiguousarray(pixels, dtype=np.int32)
+            n = pixels.size
+        else:
+            n = W * H
+        rgb = np.empty((n, 3), dtype=np.float32)
+        depth = np.empty(n, dtype=np.float32)
+        occ_arr = None if occ is None else np.ascontiguousarray(occ, dtype=np.uint32)
+        samples = self.lib.oracle_render_f32(self.h, _ptr(occ_arr), M.ctypes.data, W, H, focal, _ptr(pixels), n,
+                                             rgb.ctypes.data, depth.ctypes.data, nthreads or os.cpu_count() or 1)
         return rgb, depth, samples
 
     def rays(self, views, pairs):
