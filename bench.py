@@ -485,6 +485,8 @@ def run_glue(dev, peaks):
             torch.cuda.synchronize()
             img = rgb[0].cpu().numpy()
             oy, ou, ov = oracle.rgb24_to_yuv420p(img, w, h, 3 * w, ls)
+            to_yuv(0)  # the timed gray8 loop reused the YUV buffers
+            torch.cuda.synchronize()
             got = yuv[0].cpu().numpy()
             exact = (np.array_equal(got[:ls[0] * h], oy) and np.array_equal(got[ls[0] * h:ls[0] * h + ls[1] * ch], ou)
                      and np.array_equal(got[ls[0] * h + ls[1] * ch:], ov))

@@ -230,8 +230,8 @@ int nes_copy_to_host(void *host_dst, const void *dev_src, size_t n);
  * No counterpart in neserver (which only renders); this is the training
  * form of the renderer: a hand-written backward through the volume
  * rendering (per-sample compositing adjoint from recorded sample states),
- * the MLPs (per-sample backpropagation; weight gradients as split-K
- * reductions over the samples) and the hash grid (atomic float2 scatter-add
+ * the MLPs (per-sample backpropagation; weight gradients as GEMMs over the
+ * samples on the tensor cores, or exact FP32 reductions) and the hash grid (atomic float2 scatter-add
  * into an FP32 gradient table), then Adam on the student context's FP32
  * table and weights.  The occupancy grid is left as it is (rebuild it with
  * nes_rebuild_occupancy between steps where wanted).
@@ -245,9 +245,11 @@ typedef struct nes_train_config {
   uint32_t batch_rays;  /* rays per step (2^18 in the refit configuration) */
   float lr, beta1, beta2, eps;
   float depth_weight;
+  int32_t exact_weight_grads; /* 0: weight gradients as TF32 tensor-core GEMMs (tcgen05), 1: FP32 CUDA cores */
 } nes_train_config;
 
-/* lr 1e-2, betas (0.9, 0.99), eps 1e-15, depth weight 0.1, 2^18 rays. */
+/* lr 1e-2, betas (0.9, 0.99), eps 1e-15, depth weight 0.1, 2^18 rays,
+ * tensor-core weight gradients. */
 void nes_train_config_default(nes_train_config *cfg);
 
 /* The student must be an NES_PREC_FP32 context; its table and weights are

@@ -75,41 +75,210 @@ gray8_to_yuv420p_kernel(const uint8_t* __restrict__ g, int w, int h, int g_ls, u
   V[(size_t)cy * ls2 + cx] = 128;
 }
 
+// Vector form of the two YUV kernels: one thread per 8x2 pixel block (four
+// chroma samples), 8-byte row loads and stores, 4-byte chroma stores.  Used
+// when every base pointer and linesize is aligned (RGB/GRAY/Y to 8 bytes,
+// U/V to 4); blocks that reach past the right or bottom edge take the
+// per-sample path of the kernels above, so results are identical.
+__device__ __forceinline__ void rgb_block_scalar(const uint8_t* __restrict__ rgb, int w, int h, int rgb_ls,
+                                                 uint8_t* __restrict__ Y, uint8_t* __restrict__ U,
+                                                 uint8_t* __restrict__ V, int ls0, int ls1, int ls2, int cx,
+                                                 int cy) {
+  int sr = 0, sg = 0, sb = 0;
+#pragma unroll
+  for (int dy = 0; dy < 2; ++dy) {
+    const int yy = 2 * cy + dy;
+    const uint8_t* row = rgb + (size_t)min(yy, h - 1) * rgb_ls;
+#pragma unroll
+    for (int dx = 0; dx < 2; ++dx) {
+      const int xx = 2 * cx + dx;
+      const int rx = min(xx, w - 1);
+      const int r = row[3 * rx], g = row[3 * rx + 1], b = row[3 * rx + 2];
+      sr += r;
+      sg += g;
+      sb += b;
+      if (yy < h && xx < w) Y[(size_t)yy * ls0 + xx] = luma(r, g, b);
+    }
+  }
+  U[(size_t)cy * ls1 + cx] = clamp8((kUR * sr + kUG * sg + kUB * sb + (128 << 18) + (1 << 17)) >> 18);
+  V[(size_t)cy * ls2 + cx] = clamp8((kVR * sr + kVG * sg + kVB * sb + (128 << 18) + (1 << 17)) >> 18);
+}
+
+__global__ void __launch_bounds__(kGlueThreads)
+rgb24_to_yuv420p_v8_kernel(const uint8_t* __restrict__ rgb, int w, int h, int rgb_ls, uint8_t* __restrict__ Y,
+                           uint8_t* __restrict__ U, uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
+  const int cw = (w + 1) >> 1, ch = (h + 1) >> 1;
+  const int cx0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int cy = blockIdx.y;
+  if (cx0 >= cw || cy >= ch) return;
+  const int x0 = 2 * cx0;
+  if (x0 + 8 > w || 2 * cy + 1 >= h) {
+    for (int cx = cx0; cx < min(cx0 + 4, cw); ++cx) rgb_block_scalar(rgb, w, h, rgb_ls, Y, U, V, ls0, ls1, ls2, cx, cy);
+    return;
+  }
+  uint32_t px[2][6];  // two rows of 8 RGB pixels (24 bytes each)
+#pragma unroll
+  for (int dy = 0; dy < 2; ++dy) {
+    const uint2* p = reinterpret_cast<const uint2*>(rgb + (size_t)(2 * cy + dy) * rgb_ls + 3 * x0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const uint2 v = __ldg(p + k);
+      px[dy][2 * k] = v.x;
+      px[dy][2 * k + 1] = v.y;
+    }
+  }
+  int sr[4] = {0, 0, 0, 0}, sg[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int dy = 0; dy < 2; ++dy) {
+    uint32_t yw[2] = {0u, 0u};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = (px[dy][(3 * i) >> 2] >> (8 * ((3 * i) & 3))) & 0xff;
+      const int g = (px[dy][(3 * i + 1) >> 2] >> (8 * ((3 * i + 1) & 3))) & 0xff;
+      const int b = (px[dy][(3 * i + 2) >> 2] >> (8 * ((3 * i + 2) & 3))) & 0xff;
+      yw[i >> 2] |= (uint32_t)luma(r, g, b) << (8 * (i & 3));
+      sr[i >> 1] += r;
+      sg[i >> 1] += g;
+      sb[i >> 1] += b;
+    }
+    *reinterpret_cast<uint2*>(Y + (size_t)(2 * cy + dy) * ls0 + x0) = make_uint2(yw[0], yw[1]);
+  }
+  uint32_t uw = 0u, vw = 0u;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    uw |= (uint32_t)clamp8((kUR * sr[c] + kUG * sg[c] + kUB * sb[c] + (128 << 18) + (1 << 17)) >> 18) << (8 * c);
+    vw |= (uint32_t)clamp8((kVR * sr[c] + kVG * sg[c] + kVB * sb[c] + (128 << 18) + (1 << 17)) >> 18) << (8 * c);
+  }
+  *reinterpret_cast<uint32_t*>(U + (size_t)cy * ls1 + cx0) = uw;
+  *reinterpret_cast<uint32_t*>(V + (size_t)cy * ls2 + cx0) = vw;
+}
+
+__global__ void __launch_bounds__(kGlueThreads)
+gray8_to_yuv420p_v8_kernel(const uint8_t* __restrict__ g, int w, int h, int g_ls, uint8_t* __restrict__ Y,
+                           uint8_t* __restrict__ U, uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
+  const int cw = (w + 1) >> 1, ch = (h + 1) >> 1;
+  const int cx0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int cy = blockIdx.y;
+  if (cx0 >= cw || cy >= ch) return;
+  constexpr int32_t ys = kYR + kYG + kYB;
+  const int x0 = 2 * cx0;
+  if (x0 + 8 > w || 2 * cy + 1 >= h) {
+    for (int dy = 0; dy < 2; ++dy) {
+      const int yy = 2 * cy + dy;
+      if (yy >= h) break;
+      for (int xx = x0; xx < min(x0 + 8, w); ++xx)
+        Y[(size_t)yy * ls0 + xx] = clamp8((ys * g[(size_t)yy * g_ls + xx] + (16 << 16) + (1 << 15)) >> 16);
+    }
+    for (int cx = cx0; cx < min(cx0 + 4, cw); ++cx) {
+      U[(size_t)cy * ls1 + cx] = 128;
+      V[(size_t)cy * ls2 + cx] = 128;
+    }
+    return;
+  }
+#pragma unroll
+  for (int dy = 0; dy < 2; ++dy) {
+    const uint2 v = __ldg(reinterpret_cast<const uint2*>(g + (size_t)(2 * cy + dy) * g_ls + x0));
+    const uint32_t in[2] = {v.x, v.y};
+    uint32_t yw[2] = {0u, 0u};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int gv = (in[i >> 2] >> (8 * (i & 3))) & 0xff;
+      yw[i >> 2] |= (uint32_t)clamp8((ys * gv + (16 << 16) + (1 << 15)) >> 16) << (8 * (i & 3));
+    }
+    *reinterpret_cast<uint2*>(Y + (size_t)(2 * cy + dy) * ls0 + x0) = make_uint2(yw[0], yw[1]);
+  }
+  *reinterpret_cast<uint32_t*>(U + (size_t)cy * ls1 + cx0) = 0x80808080u;
+  *reinterpret_cast<uint32_t*>(V + (size_t)cy * ls2 + cx0) = 0x80808080u;
+}
+
 // round-half-up of d * 1000 in FP32; NaN/negative -> 0; saturate at 65535.
-__global__ void depth_pack_u16mm_kernel(const float* __restrict__ d, size_t n, uint16_t* __restrict__ out) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float mm = __fmul_rn(d[i], 1000.0f);
-    uint16_t q;
-    if (!(mm >= 0.0f))
-      q = 0;
-    else if (mm >= 65535.0f)
-      q = 65535;
-    else
-      q = (uint16_t)__float2uint_rz(__fadd_rn(mm, 0.5f));
-    out[i] = q;
-  }
+__device__ __forceinline__ uint16_t pack_mm(float d) {
+  const float mm = __fmul_rn(d, 1000.0f);
+  if (!(mm >= 0.0f)) return 0;
+  if (mm >= 65535.0f) return 65535;
+  return (uint16_t)__float2uint_rz(__fadd_rn(mm, 0.5f));
 }
 
-__global__ void depth_to_gray8_kernel(const float* __restrict__ d, size_t n, float dmax, uint8_t* __restrict__ out) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float q = __fdiv_rn(d[i], dmax);
-    const float c = q > 0.0f ? (q < 1.0f ? q : 1.0f) : 0.0f;
-    out[i] = (uint8_t)__float2uint_rz(__fadd_rn(__fmul_rn(c, 255.0f), 0.5f));
-  }
+__device__ __forceinline__ uint8_t gray_q(float d, float dmax) {
+  const float q = __fdiv_rn(d, dmax);
+  const float c = q > 0.0f ? (q < 1.0f ? q : 1.0f) : 0.0f;
+  return (uint8_t)__float2uint_rz(__fadd_rn(__fmul_rn(c, 255.0f), 0.5f));
 }
 
-__global__ void rgb_to_rgb24_kernel(const float* __restrict__ rgb, size_t n, uint8_t* __restrict__ out) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float x = rgb[i];
-    const float c = x > 0.0f ? (x < 1.0f ? x : 1.0f) : 0.0f;
-    out[i] = (uint8_t)__float2uint_rz(__fadd_rn(__fmul_rn(c, 255.0f), 0.5f));
+__device__ __forceinline__ uint8_t unit_q(float x) {
+  const float c = x > 0.0f ? (x < 1.0f ? x : 1.0f) : 0.0f;
+  return (uint8_t)__float2uint_rz(__fadd_rn(__fmul_rn(c, 255.0f), 0.5f));
+}
+
+// Elementwise kernels: four elements per step with a float4 load when the
+// input is 16-byte aligned and the output aligned to its 4-element store
+// (the host checks), elements past the last whole group scalar.
+__global__ void depth_pack_u16mm_kernel(const float* __restrict__ d, size_t n, uint16_t* __restrict__ out, int vec) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t done = 0;
+  if (vec) {
+    const size_t n4 = n / 4;
+    for (size_t i = i0; i < n4; i += stride) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(d) + i);
+      reinterpret_cast<uint2*>(out)[i] =
+          make_uint2((uint32_t)pack_mm(v.x) | ((uint32_t)pack_mm(v.y) << 16),
+                     (uint32_t)pack_mm(v.z) | ((uint32_t)pack_mm(v.w) << 16));
+    }
+    done = n4 * 4;
   }
+  for (size_t i = done + i0; i < n; i += stride) out[i] = pack_mm(d[i]);
+}
+
+__global__ void depth_to_gray8_kernel(const float* __restrict__ d, size_t n, float dmax, uint8_t* __restrict__ out,
+                                      int vec) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t done = 0;
+  if (vec) {
+    const size_t n4 = n / 4;
+    for (size_t i = i0; i < n4; i += stride) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(d) + i);
+      reinterpret_cast<uint32_t*>(out)[i] = (uint32_t)gray_q(v.x, dmax) | ((uint32_t)gray_q(v.y, dmax) << 8) |
+                                            ((uint32_t)gray_q(v.z, dmax) << 16) | ((uint32_t)gray_q(v.w, dmax) << 24);
+    }
+    done = n4 * 4;
+  }
+  for (size_t i = done + i0; i < n; i += stride) out[i] = gray_q(d[i], dmax);
+}
+
+__global__ void rgb_to_rgb24_kernel(const float* __restrict__ rgb, size_t n, uint8_t* __restrict__ out, int vec) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t done = 0;
+  if (vec) {
+    const size_t n4 = n / 4;
+    for (size_t i = i0; i < n4; i += stride) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(rgb) + i);
+      reinterpret_cast<uint32_t*>(out)[i] = (uint32_t)unit_q(v.x) | ((uint32_t)unit_q(v.y) << 8) |
+                                            ((uint32_t)unit_q(v.z) << 16) | ((uint32_t)unit_q(v.w) << 24);
+    }
+    done = n4 * 4;
+  }
+  for (size_t i = done + i0; i < n; i += stride) out[i] = unit_q(rgb[i]);
 }
 
 unsigned grid_for(size_t n) {
-  size_t b = (n + kGlueThreads - 1) / kGlueThreads;
-  if (b > 152 * 32) b = 152 * 32;  // grid-stride beyond 32 resident blocks per SM
+  size_t b = (n + 4 * kGlueThreads - 1) / (4 * kGlueThreads);
+  if (b > 152 * 8) b = 152 * 8;  // grid-stride beyond 8 resident blocks per SM
   return (unsigned)(b ? b : 1);
+}
+
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+}  // namespace
+
+namespace {
+
+bool yuv_vec_ok(const uint8_t* src, int src_ls, const uint8_t* y, const uint8_t* u, const uint8_t* v,
+                const int ls[3]) {
+  return aligned(src, 8) && src_ls % 8 == 0 && aligned(y, 8) && ls[0] % 8 == 0 && aligned(u, 4) && ls[1] % 4 == 0 &&
+         aligned(v, 4) && ls[2] % 4 == 0;
 }
 
 }  // namespace
@@ -117,31 +286,43 @@ unsigned grid_for(size_t n) {
 cudaError_t launch_rgb24_to_yuv420p(const uint8_t* rgb, int w, int h, int rgb_ls, uint8_t* y, uint8_t* u,
                                     uint8_t* v, const int ls[3], cudaStream_t stream) {
   const int cw = (w + 1) / 2, ch = (h + 1) / 2;
-  dim3 grid((cw + kGlueThreads - 1) / kGlueThreads, ch);
-  rgb24_to_yuv420p_kernel<<<grid, kGlueThreads, 0, stream>>>(rgb, w, h, rgb_ls, y, u, v, ls[0], ls[1], ls[2]);
+  if (yuv_vec_ok(rgb, rgb_ls, y, u, v, ls)) {
+    const int groups = (cw + 3) / 4;
+    dim3 grid((groups + kGlueThreads - 1) / kGlueThreads, ch);
+    rgb24_to_yuv420p_v8_kernel<<<grid, kGlueThreads, 0, stream>>>(rgb, w, h, rgb_ls, y, u, v, ls[0], ls[1], ls[2]);
+  } else {
+    dim3 grid((cw + kGlueThreads - 1) / kGlueThreads, ch);
+    rgb24_to_yuv420p_kernel<<<grid, kGlueThreads, 0, stream>>>(rgb, w, h, rgb_ls, y, u, v, ls[0], ls[1], ls[2]);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_gray8_to_yuv420p(const uint8_t* g, int w, int h, int g_ls, uint8_t* y, uint8_t* u, uint8_t* v,
                                     const int ls[3], cudaStream_t stream) {
   const int cw = (w + 1) / 2, ch = (h + 1) / 2;
-  dim3 grid((cw + kGlueThreads - 1) / kGlueThreads, ch);
-  gray8_to_yuv420p_kernel<<<grid, kGlueThreads, 0, stream>>>(g, w, h, g_ls, y, u, v, ls[0], ls[1], ls[2]);
+  if (yuv_vec_ok(g, g_ls, y, u, v, ls)) {
+    const int groups = (cw + 3) / 4;
+    dim3 grid((groups + kGlueThreads - 1) / kGlueThreads, ch);
+    gray8_to_yuv420p_v8_kernel<<<grid, kGlueThreads, 0, stream>>>(g, w, h, g_ls, y, u, v, ls[0], ls[1], ls[2]);
+  } else {
+    dim3 grid((cw + kGlueThreads - 1) / kGlueThreads, ch);
+    gray8_to_yuv420p_kernel<<<grid, kGlueThreads, 0, stream>>>(g, w, h, g_ls, y, u, v, ls[0], ls[1], ls[2]);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_depth_pack_u16mm(const float* d, size_t n, uint16_t* out, cudaStream_t stream) {
-  depth_pack_u16mm_kernel<<<grid_for(n), kGlueThreads, 0, stream>>>(d, n, out);
+  depth_pack_u16mm_kernel<<<grid_for(n), kGlueThreads, 0, stream>>>(d, n, out, aligned(d, 16) && aligned(out, 8));
   return cudaGetLastError();
 }
 
 cudaError_t launch_depth_to_gray8(const float* d, size_t n, float dmax, uint8_t* out, cudaStream_t stream) {
-  depth_to_gray8_kernel<<<grid_for(n), kGlueThreads, 0, stream>>>(d, n, dmax, out);
+  depth_to_gray8_kernel<<<grid_for(n), kGlueThreads, 0, stream>>>(d, n, dmax, out, aligned(d, 16) && aligned(out, 4));
   return cudaGetLastError();
 }
 
 cudaError_t launch_rgb_to_rgb24(const float* rgb, size_t n, uint8_t* out, cudaStream_t stream) {
-  rgb_to_rgb24_kernel<<<grid_for(n), kGlueThreads, 0, stream>>>(rgb, n, out);
+  rgb_to_rgb24_kernel<<<grid_for(n), kGlueThreads, 0, stream>>>(rgb, n, out, aligned(rgb, 16) && aligned(out, 4));
   return cudaGetLastError();
 }
 

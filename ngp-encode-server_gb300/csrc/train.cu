@@ -40,6 +40,7 @@
 #include "kernels.h"
 #include "mlp32.cuh"
 #include "nes_gb300.h"
+#include "tc_ptx.cuh"
 
 using namespace nes;
 
@@ -71,20 +72,28 @@ struct SampleRec {  // compacted sample with its compositing adjoint
 };
 
 // Per-sample staging of the weight-gradient reductions, in 32-sample
-// tiles: feature f of sample s of an F-wide array at
-// ((s / 32) * F + f) * 32 + s % 32.  A warp's store of one feature is 128
-// contiguous bytes, a thread's features sit at small immediate offsets
-// from one base, and a tile of all F features is one contiguous block.
+// tiles.  Each tile of an F-wide array (F a multiple of 8) is one
+// contiguous block of F x 32 floats in the canonical K-major layout of the
+// tensor core's shared-memory operands, no swizzle, K = sample: 8-feature x
+// 4-sample core matrices of 128 bytes, the 8 core matrices of a feature
+// group along K at 128-byte steps, feature groups at 1,024-byte steps.
+// Feature f of sample k of a tile sits at float
+//   (f / 8) * 256 + (k / 4) * 32 + (f % 8) * 4 + k % 4,
+// so one bulk copy per array and tile lands a ready MMA operand, and a
+// thread's features sit at immediate offsets from one base.
 constexpr int kStageFloats = kEnc + kHid + kCIn + kHid + kHid  // activations: enc, h1, cin, g1, g2
-                             + kHid + kDOut + kHid + kHid + 4;  // deltas: dh1, dout, dg1, dg2, dlogit(3)+pad
+                             + kHid + kDOut + kHid + kHid + 8;  // deltas: dh1, dout, dg1, dg2, dlogit(3)+zeros
 struct Staging {
   float *enc, *h1, *cin, *g1, *g2;       // F = 32, 64, 32, 64, 64
-  float *dh1, *dout, *dg1, *dg2, *dlog;  // F = 64, 16, 64, 64, 4 (feature 3 unused)
+  float *dh1, *dout, *dg1, *dg2, *dlog;  // F = 64, 16, 64, 64, 8 (features 3..7 zero)
 };
+constexpr int kFDlog = 8;
 
 __device__ __forceinline__ float* stage_row(float* a, int F, uint32_t s) {
-  return a + ((size_t)(s >> 5) * F) * 32 + (s & 31u);
+  const uint32_t k = s & 31u;
+  return a + (size_t)(s >> 5) * F * 32 + (k >> 2) * 32 + (k & 3);
 }
+__host__ __device__ constexpr int soff(int f) { return (f >> 3) * 256 + (f & 7) * 4; }
 
 // Forward: 128-thread blocks, three resident per SM at its 135 registers.
 // Backward: 256-thread blocks capped at 128 registers, two resident per SM
@@ -278,7 +287,7 @@ adjoint_kernel(const TrainRay* __restrict__ rays, const RayOut* __restrict__ rou
 
 // Backward, thread per record of the chunk [first, first + count).
 // Activations stay in registers (ReLU masks as 64-bit words); every staged
-// value is written once, feature f of the sample at row[32 f].
+// value is written once, feature f of the sample at row[soff(f)].
 __device__ __forceinline__ float dot64(const float* __restrict__ w, const float in[64]) {
   const float4* w4 = reinterpret_cast<const float4*>(w);
   float a = 0.0f;
@@ -313,7 +322,16 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
   }
   __syncthreads();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= count) return;
+  if (s >= ((count + 31u) & ~31u)) return;
+  if (s >= count) {  // rows of the last tile past the chunk's samples: zeros for the reductions
+    float* const arr[10] = {st.enc, st.h1, st.cin, st.g1, st.g2, st.dh1, st.dout, st.dg1, st.dg2, st.dlog};
+    const int F[10] = {kEnc, kHid, kCIn, kHid, kHid, kHid, kDOut, kHid, kHid, 8};
+    for (int a = 0; a < 10; ++a) {
+      float* r = stage_row(arr[a], F[a], s);
+      for (int f = 0; f < F[a]; ++f) r[soff(f)] = 0.0f;
+    }
+    return;
+  }
   const SampleRec q = recs[first + s];
   const float3 x = make_float3(q.x, q.y, q.z);
   float* const r_enc = stage_row(st.enc, kEnc, s);
@@ -325,12 +343,12 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
   float* const r_dout = stage_row(st.dout, kDOut, s);
   float* const r_dg1 = stage_row(st.dg1, kHid, s);
   float* const r_dg2 = stage_row(st.dg2, kHid, s);
-  float* const r_dlog = stage_row(st.dlog, 4, s);
+  float* const r_dlog = stage_row(st.dlog, 8, s);
   // ---- forward recompute ----
   float enc[kEnc];
   encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
 #pragma unroll
-  for (int k = 0; k < kEnc; ++k) r_enc[32 * k] = enc[k];
+  for (int k = 0; k < kEnc; ++k) r_enc[soff(k)] = enc[k];
   float out[kDOut];
 #pragma unroll
   for (int m = 0; m < kDOut; ++m) out[m] = 0.0f;
@@ -338,7 +356,7 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
 #pragma unroll 1
   for (int j = 0; j < kHid; ++j) {
     const float a = fmaxf(dot32(W.dw1 + j * kEnc, enc), 0.0f);
-    r_h1[32 * j] = a;
+    r_h1[soff(j)] = a;
     m_h1 |= (uint64_t)(a > 0.0f) << j;
     const float4* w2 = reinterpret_cast<const float4*>(W.dw2t + j * kDOut);
 #pragma unroll
@@ -360,12 +378,12 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
   for (int k = 0; k < 15; ++k) cin[16 + k] = out[1 + k];
   cin[31] = 0.0f;
 #pragma unroll
-  for (int k = 0; k < kCIn; ++k) r_cin[32 * k] = cin[k];
+  for (int k = 0; k < kCIn; ++k) r_cin[soff(k)] = cin[k];
   float g[kHid];  // g1, then its gradient
 #pragma unroll
   for (int j = 0; j < kHid; ++j) {
     g[j] = fmaxf(dot32(W.cw1 + j * kCIn, cin), 0.0f);
-    r_g1[32 * j] = g[j];
+    r_g1[soff(j)] = g[j];
   }
   uint64_t m_g1 = 0;
 #pragma unroll
@@ -375,7 +393,7 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
 #pragma unroll 1
   for (int j = 0; j < kHid; ++j) {
     const float a = fmaxf(dot64(W.cw2 + j * kHid, g), 0.0f);
-    r_g2[32 * j] = a;
+    r_g2[soff(j)] = a;
     m_g2 |= (uint64_t)(a > 0.0f) << j;
     const float4 c3 = *reinterpret_cast<const float4*>(W.cw3t + j * 4);
     lg0 = fmaf(c3.x, a, lg0);
@@ -385,16 +403,18 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
   // ---- backward ----
   const float c0 = sigmoidf(lg0), c1 = sigmoidf(lg1), c2 = sigmoidf(lg2);
   const float dl0 = q.dcr * c0 * (1.0f - c0), dl1 = q.dcg * c1 * (1.0f - c1), dl2 = q.dcb * c2 * (1.0f - c2);
-  r_dlog[0] = dl0;
-  r_dlog[32] = dl1;
-  r_dlog[64] = dl2;
+  r_dlog[soff(0)] = dl0;
+  r_dlog[soff(1)] = dl1;
+  r_dlog[soff(2)] = dl2;
+#pragma unroll
+  for (int f = 3; f < 8; ++f) r_dlog[soff(f)] = 0.0f;
 #pragma unroll
   for (int k = 0; k < kHid; ++k) g[k] = 0.0f;
 #pragma unroll 1
   for (int j = 0; j < kHid; ++j) {  // dg2_j, and dg1 += cw2[j][:] dg2_j
     const float4 c3 = *reinterpret_cast<const float4*>(W.cw3t + j * 4);
     const float d2 = ((m_g2 >> j) & 1) ? fmaf(c3.x, dl0, fmaf(c3.y, dl1, c3.z * dl2)) : 0.0f;
-    r_dg2[32 * j] = d2;
+    r_dg2[soff(j)] = d2;
     const float4* w4 = reinterpret_cast<const float4*>(W.cw2 + j * kHid);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
@@ -408,14 +428,14 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
 #pragma unroll
   for (int k = 0; k < kHid; ++k) {
     g[k] = ((m_g1 >> k) & 1) ? g[k] : 0.0f;
-    r_dg1[32 * k] = g[k];
+    r_dg1[soff(k)] = g[k];
   }
   float dout[kDOut];
   dout[0] = q.dsigma * sigma;
 #pragma unroll
   for (int m = 0; m < 15; ++m) dout[1 + m] = dot64(S.cw1g + m * kHid, g);
 #pragma unroll
-  for (int m = 0; m < kDOut; ++m) r_dout[32 * m] = dout[m];
+  for (int m = 0; m < kDOut; ++m) r_dout[soff(m)] = dout[m];
   float denc[kEnc];
 #pragma unroll
   for (int k = 0; k < kEnc; ++k) denc[k] = 0.0f;
@@ -432,7 +452,7 @@ backward_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t cou
       a = fmaf(w.w, dout[4 * k + 3], a);
     }
     const float dh = ((m_h1 >> j) & 1) ? a : 0.0f;
-    r_dh1[32 * j] = dh;
+    r_dh1[soff(j)] = dh;
     const float4* w1 = reinterpret_cast<const float4*>(W.dw1 + j * kEnc);
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -491,12 +511,12 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
   const uint32_t lo = blockIdx.x * per, hi = min(S, lo + per);
   for (uint32_t base = lo; base < hi; base += kDwTile) {
     const uint32_t rows = min((uint32_t)kDwTile, hi - base);
-    // The tile is one contiguous block: float4 loads of 4 samples of one
-    // feature, stored transposed.
+    // The tile is one contiguous block: each float4 holds 4 samples of one
+    // feature (core-matrix layout), stored transposed.
     const float4* ta = reinterpret_cast<const float4*>(act + (size_t)(base / kDwTile) * IN * kDwTile);
     const float4* td = reinterpret_cast<const float4*>(delta + (size_t)(base / kDwTile) * LDD * kDwTile);
     for (int e = tid; e < kDwTile * IN / 4; e += kDwThreads) {
-      const int f = (4 * e) / kDwTile, r = (4 * e) % kDwTile;
+      const int f = (e >> 6) * 8 + (e & 7), r = ((e >> 3) & 7) * 4;
       const float4 v = ta[e];
       sa[r + 0][f] = (uint32_t)(r + 0) < rows ? v.x : 0.0f;
       sa[r + 1][f] = (uint32_t)(r + 1) < rows ? v.y : 0.0f;
@@ -504,7 +524,7 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
       sa[r + 3][f] = (uint32_t)(r + 3) < rows ? v.w : 0.0f;
     }
     for (int e = tid; e < kDwTile * LDD / 4; e += kDwThreads) {
-      const int f = (4 * e) / kDwTile, r = (4 * e) % kDwTile;
+      const int f = (e >> 6) * 8 + (e & 7), r = ((e >> 3) & 7) * 4;
       const float4 v = f < OUT ? td[e] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       sd[r + 0][f] = (uint32_t)(r + 0) < rows ? v.x : 0.0f;
       sd[r + 1][f] = (uint32_t)(r + 1) < rows ? v.y : 0.0f;
@@ -532,6 +552,157 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
       for (int c = 0; c < 4; ++c)
         if (acc[p][c] != 0.0f) atomicAdd(dw + o * IN + ti * 4 + c, acc[p][c]);
   }
+}
+
+// ---------------- weight gradients on the tensor cores (kind::tf32) ----------------
+// Per 32-sample tile, two MMA groups, M = 128, K = 32 as four K = 8 steps:
+//   D1[128 x 144] += [enc | cin | h1] (rows = features) x [dh1 | dg1 | dout]^T
+//   D2[128 x  80] += [g1 | g2] x [dg2 | dlog | 0]^T
+// whose diagonal blocks are the five dW^T (D1[enc][dh1] = DW1^T, D1[cin][dg1]
+// = CW1^T, D1[h1][dout] = DW2^T, D2[g1][dg2] = CW2^T, D2[g2][dlog] = CW3^T);
+// the off-diagonal products are discarded.  D stays in TMEM across all of a
+// CTA's tiles and is added to dW once at the end.  One CTA per SM: warp 0
+// lane 0 streams tiles into a 3-stage ring with bulk copies (one per array,
+// the staging is already in the operand layout), warp 1 lane 0 issues the
+// MMAs and releases stages by tcgen05.commit, all four warps read D back.
+// The kernel is bound by reading the staging (60,416 B per tile).
+constexpr int kTcStages = 3;
+constexpr uint32_t kA1Bytes = 128 * 128, kB1Bytes = 144 * 128, kA2Bytes = 128 * 128, kB2Bytes = 80 * 128;
+constexpr uint32_t kStageBytes = kA1Bytes + kB1Bytes + kA2Bytes + kB2Bytes;
+constexpr uint32_t kTileTx = (kEnc + kCIn + kHid + kHid + kHid + kDOut + kHid + kHid + kHid + kFDlog) * 128;
+constexpr uint32_t kD1Col = 0, kD2Col = 144, kTmemCols = 256;
+constexpr int kDwTcThreads = 128;
+constexpr uint32_t kErrTimeout = 4u;
+
+struct DwTcSmem {
+  uint8_t stage[kTcStages][kStageBytes];
+  uint64_t full[kTcStages], empty[kTcStages], done;
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kDwTcThreads, 1)
+dw_tc_kernel(Staging st, uint32_t ntiles, float* __restrict__ dw, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(128) uint8_t smem_dw[];
+  DwTcSmem& S = *reinterpret_cast<DwTcSmem*>(smem_dw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+  const uint32_t t0 = blockIdx.x * per, t1 = min(ntiles, t0 + per);
+  if (t1 <= t0) return;  // uniform over the CTA, before any barrier or TMEM use
+  const uint32_t my = t1 - t0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kTcStages; ++i) {
+      tc::mbar_init(&S.full[i], 1);
+      tc::mbar_init(&S.empty[i], 1);
+    }
+    tc::mbar_init(&S.done, 1);
+    tc::fence_mbar_init();
+  }
+  // B2 rows 72..79 are never copied: zero in every stage.
+  for (int i = threadIdx.x; i < kTcStages * 256; i += blockDim.x)
+    reinterpret_cast<float*>(S.stage[i / 256] + kA1Bytes + kB1Bytes + kA2Bytes + 72 * 128)[i % 256] = 0.0f;
+  tc::fence_async_smem();
+  if (warp == 1) {
+    tc::tmem_alloc(&S.tmem_base, kTmemCols);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = S.tmem_base;
+  if (warp == 0 && lane == 0) {  // producer
+    uint32_t issued = 0;
+    bool ok = true;
+    for (uint32_t i = 0; i < my; ++i) {
+      const int sidx = (int)(i % kTcStages);
+      if (i >= (uint32_t)kTcStages && !tc::mbar_wait_sleep(&S.empty[sidx], ((i / kTcStages) & 1u) ^ 1u)) {
+        ok = false;
+        break;
+      }
+      uint8_t* a1 = S.stage[sidx];
+      uint8_t* b1 = a1 + kA1Bytes;
+      uint8_t* a2 = b1 + kB1Bytes;
+      uint8_t* b2 = a2 + kA2Bytes;
+      const size_t t = t0 + i;
+      uint64_t* bar = &S.full[sidx];
+      tc::mbar_arrive_expect_tx(bar, kTileTx);
+      tc::bulk_g2s(a1, st.enc + t * kEnc * 32, kEnc * 128, bar);
+      tc::bulk_g2s(a1 + kEnc * 128, st.cin + t * kCIn * 32, kCIn * 128, bar);
+      tc::bulk_g2s(a1 + (kEnc + kCIn) * 128, st.h1 + t * kHid * 32, kHid * 128, bar);
+      tc::bulk_g2s(b1, st.dh1 + t * kHid * 32, kHid * 128, bar);
+      tc::bulk_g2s(b1 + kHid * 128, st.dg1 + t * kHid * 32, kHid * 128, bar);
+      tc::bulk_g2s(b1 + 2 * kHid * 128, st.dout + t * kDOut * 32, kDOut * 128, bar);
+      tc::bulk_g2s(a2, st.g1 + t * kHid * 32, kHid * 128, bar);
+      tc::bulk_g2s(a2 + kHid * 128, st.g2 + t * kHid * 32, kHid * 128, bar);
+      tc::bulk_g2s(b2, st.dg2 + t * kHid * 32, kHid * 128, bar);
+      tc::bulk_g2s(b2 + kHid * 128, st.dlog + t * kFDlog * 32, kFDlog * 128, bar);
+      ++issued;
+    }
+    if (!ok) atomicExch(err, kErrTimeout);
+    // Copies still in flight land before the CTA may exit: wait (bounded)
+    // for the last issued tile of every stage.
+    for (uint32_t k = 0; k < (uint32_t)kTcStages && k < issued; ++k) {
+      const uint32_t i = issued - 1 - k;
+      if (!tc::mbar_wait_sleep(&S.full[i % kTcStages], (i / kTcStages) & 1u)) atomicExch(err, kErrTimeout);
+    }
+  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    constexpr uint32_t id1 = tc::idesc_tf32_f32(128, 144), id2 = tc::idesc_tf32_f32(128, 80);
+    for (uint32_t i = 0; i < my; ++i) {
+      const int sidx = (int)(i % kTcStages);
+      if (!tc::mbar_wait_sleep(&S.full[sidx], (i / kTcStages) & 1u)) {
+        atomicExch(err, kErrTimeout);
+        break;
+      }
+      tc::fence_after();
+      const uint32_t a1 = tc::smem_addr(S.stage[sidx]), b1 = a1 + kA1Bytes, a2 = b1 + kB1Bytes, b2 = a2 + kA2Bytes;
+#pragma unroll
+      for (uint32_t kk = 0; kk < 4; ++kk) {
+        const uint32_t acc = (i > 0 || kk > 0) ? 1u : 0u;
+        tc::mma_tf32(tmem + kD1Col, tc::sdesc(a1 + kk * 256, 128, 1024), tc::sdesc(b1 + kk * 256, 128, 1024), id1, acc);
+        tc::mma_tf32(tmem + kD2Col, tc::sdesc(a2 + kk * 256, 128, 1024), tc::sdesc(b2 + kk * 256, 128, 1024), id2, acc);
+      }
+      tc::mma_commit(&S.empty[sidx]);
+    }
+    tc::mma_commit(&S.done);
+  }
+  __syncwarp();
+  // Epilogue: warp w owns TMEM lanes 32w..32w+31 (rows of D1 and D2).
+  const bool done = tc::mbar_wait_sleep(&S.done, 0);
+  tc::fence_after();
+  if (!done) {
+    if (lane == 0) atomicExch(err, kErrTimeout);
+  } else {
+    const uint32_t lanes = tmem + ((uint32_t)(warp * 32) << 16);
+    const int row = warp * 32 + lane;
+    float v[32];
+    if (warp == 0) {  // D1 rows 0..31: enc feature `row` x dh1 j -> DW1[j][row]
+      for (int c = 0; c < 2; ++c) {
+        tc::tmem_ld32(lanes + kD1Col + 32 * c, v);
+        for (int j = 0; j < 32; ++j) atomicAdd(dw + kOffDW1 + (32 * c + j) * kEnc + row, v[j]);
+      }
+    } else if (warp == 1) {  // D1 rows 32..63: cin feature row-32 x dg1 j -> CW1[j][row-32]
+      for (int c = 0; c < 2; ++c) {
+        tc::tmem_ld32(lanes + kD1Col + 64 + 32 * c, v);
+        for (int j = 0; j < 32; ++j) atomicAdd(dw + kOffCW1 + (32 * c + j) * kCIn + (row - 32), v[j]);
+      }
+    } else {  // D1 rows 64..127: h1 feature row-64 x dout m -> DW2[m][row-64]
+      float u[16];
+      tc::tmem_ld16(lanes + kD1Col + 128, u);
+      for (int m = 0; m < kDOut; ++m) atomicAdd(dw + kOffDW2 + m * kHid + (row - 64), u[m]);
+    }
+    if (warp < 2) {  // D2 rows 0..63: g1 feature `row` x dg2 j -> CW2[j][row]
+      for (int c = 0; c < 2; ++c) {
+        tc::tmem_ld32(lanes + kD2Col + 32 * c, v);
+        for (int j = 0; j < 32; ++j) atomicAdd(dw + kOffCW2 + (32 * c + j) * kHid + row, v[j]);
+      }
+    } else {  // D2 rows 64..127: g2 feature row-64 x dlog c -> CW3[c][row-64]
+      float u[16];
+      tc::tmem_ld16(lanes + kD2Col + 64, u);
+      for (int c = 0; c < 3; ++c) atomicAdd(dw + kOffCW3 + c * kHid + (row - 64), u[c]);
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 1) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
 __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -746,11 +917,25 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
     backward_kernel<<<(cnt + kBwdThreads - 1) / kBwdThreads, kBwdThreads, kSmemB, t->st>>>(t->d_recs, first, cnt, t->d_rays,
                                                                                   c->scene, sg, t->d_gtable);
     TR_CUDA(cudaGetLastError());
-    TR_CUDA((launch_dw<kEnc, kHid, kHid>(sg.enc, sg.dh1, cnt, gw + kOffDW1, sms, t->st)));
-    TR_CUDA((launch_dw<kHid, kDOut, kDOut>(sg.h1, sg.dout, cnt, gw + kOffDW2, sms, t->st)));
-    TR_CUDA((launch_dw<kCIn, kHid, kHid>(sg.cin, sg.dg1, cnt, gw + kOffCW1, sms, t->st)));
-    TR_CUDA((launch_dw<kHid, kHid, kHid>(sg.g1, sg.dg2, cnt, gw + kOffCW2, sms, t->st)));
-    TR_CUDA((launch_dw<kHid, 3, 4>(sg.g2, sg.dlog, cnt, gw + kOffCW3, sms, t->st)));
+    if (t->cfg.exact_weight_grads) {
+      TR_CUDA((launch_dw<kEnc, kHid, kHid>(sg.enc, sg.dh1, cnt, gw + kOffDW1, sms, t->st)));
+      TR_CUDA((launch_dw<kHid, kDOut, kDOut>(sg.h1, sg.dout, cnt, gw + kOffDW2, sms, t->st)));
+      TR_CUDA((launch_dw<kCIn, kHid, kHid>(sg.cin, sg.dg1, cnt, gw + kOffCW1, sms, t->st)));
+      TR_CUDA((launch_dw<kHid, kHid, kHid>(sg.g1, sg.dg2, cnt, gw + kOffCW2, sms, t->st)));
+      TR_CUDA((launch_dw<kHid, 3, kFDlog>(sg.g2, sg.dlog, cnt, gw + kOffCW3, sms, t->st)));
+    } else {
+      const uint32_t tiles = (cnt + 31) / 32;
+      const uint32_t grid = tiles < (uint32_t)sms ? tiles : (uint32_t)sms;
+      dw_tc_kernel<<<grid, kDwTcThreads, sizeof(DwTcSmem), t->st>>>(sg, tiles, gw, t->d_ctr + 1);
+      TR_CUDA(cudaGetLastError());
+    }
+  }
+  {  // a tensor-core wait that ran out reports through the error word
+    uint32_t e = 0;
+    TR_CUDA(cudaMemcpyAsync(&e, t->d_ctr + 1, sizeof(e), cudaMemcpyDeviceToHost, t->st));
+    TR_CUDA(cudaStreamSynchronize(t->st));
+    if (e == kErrTimeout) return NES_ETIMEDOUT;
+    if (e) return NES_EINVAL;
   }
   TR_CUDA(cudaEventRecord(t->ev[2], t->st));
   return NES_OK;
@@ -824,6 +1009,7 @@ void nes_train_config_default(nes_train_config* cfg) {
   cfg->beta2 = 0.99f;
   cfg->eps = 1e-15f;
   cfg->depth_weight = 0.1f;
+  cfg->exact_weight_grads = 0;
 }
 
 int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** out) {
@@ -875,7 +1061,9 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaMemset(t->d_ctr, 0, 4 * sizeof(uint32_t)) != cudaSuccess)
     return fail(NES_EIO);
   if (cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess ||
-      cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess)
+      cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess ||
+      cudaFuncSetAttribute(dw_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(DwTcSmem)) !=
+          cudaSuccess)
     return fail(NES_EIO);
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_kernel, kFwdThreads, kSmemW) != cudaSuccess)

@@ -90,7 +90,8 @@ class NesServerStats(ctypes.Structure):
 
 class NesTrainConfig(ctypes.Structure):
     _fields_ = [("batch_rays", ctypes.c_uint32), ("lr", ctypes.c_float), ("beta1", ctypes.c_float),
-                ("beta2", ctypes.c_float), ("eps", ctypes.c_float), ("depth_weight", ctypes.c_float)]
+                ("beta2", ctypes.c_float), ("eps", ctypes.c_float), ("depth_weight", ctypes.c_float),
+                ("exact_weight_grads", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p

@@ -35,8 +35,12 @@ def visible(plane, ls, w, h):
     return plane.reshape(-1, ls)[:h, :w]
 
 
+# Row strides that are multiples of 8 take the vector kernel (8x2 pixel
+# blocks); (33, 17, 5), (30, 20, 6) and (1922, 1081, 2) do so with blocks
+# cut by the right and bottom edges.  The others take the per-sample kernel.
 @pytest.mark.parametrize("w,h,pad", [(1280, 720, 0), (1920, 1080, 0), (1920, 1832, 0), (640, 360, 0),
-                                      (33, 17, 0), (31, 1, 5), (1, 1, 0), (2, 2, 3), (257, 255, 32)])
+                                      (33, 17, 0), (31, 1, 5), (1, 1, 0), (2, 2, 3), (257, 255, 32),
+                                      (33, 17, 5), (30, 20, 6), (1922, 1081, 2)])
 def test_rgb24_to_yuv420p_bit_exact(cuda, nes_lib, oracle_mod, w, h, pad):
     rng = np.random.default_rng(w * 7919 + h)
     img = synth_frame(rng, w, h)
@@ -65,13 +69,14 @@ def test_golden_yuv_on_gpu(cuda, nes_lib):
     assert np.array_equal(visible(v, ls[2], cw, ch), visible(g["v"], ls[2], cw, ch))
 
 
-@pytest.mark.parametrize("w,h", [(1280, 720), (33, 17), (1, 1)])
-def test_gray8_to_yuv420p_bit_exact(cuda, nes_lib, oracle_mod, w, h):
+@pytest.mark.parametrize("w,h,pad", [(1280, 720, 0), (33, 17, 0), (1, 1, 0), (33, 17, 7), (1922, 1081, 6)])
+def test_gray8_to_yuv420p_bit_exact(cuda, nes_lib, oracle_mod, w, h, pad):
     rng = np.random.default_rng(w + h)
-    g = rng.integers(0, 256, (h, w), dtype=np.uint8)
+    g = np.zeros((h, w + pad), np.uint8)
+    g[:, :w] = rng.integers(0, 256, (h, w), dtype=np.uint8)
     ls = nes_lib.linesizes(w)
-    gy, gu, gv = gpu_yuv(cuda, nes_lib, g, w, h, w, ls, gray=True)
-    oy, ou, ov = oracle_mod.gray8_to_yuv420p(g, w, h, w, ls)
+    gy, gu, gv = gpu_yuv(cuda, nes_lib, g, w, h, w + pad, ls, gray=True)
+    oy, ou, ov = oracle_mod.gray8_to_yuv420p(g, w, h, w + pad, ls)
     cw, ch = (w + 1) // 2, (h + 1) // 2
     assert np.array_equal(visible(gy, ls[0], w, h), visible(oy, ls[0], w, h))
     assert np.array_equal(visible(gu, ls[1], cw, ch), visible(ou, ls[1], cw, ch))
@@ -108,3 +113,31 @@ def test_rgb24_and_gray8_quantisation(cuda, nes_lib, oracle_mod):
     assert lib.nes_depth_to_gray8(src.data_ptr(), d.size, 4.0, out.data_ptr(), None) == 0
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), oracle_mod.depth_to_gray8(d, 4.0))
+
+
+@pytest.mark.parametrize("offset,extra", [(0, 1), (1, 0), (2, 3), (3, 2)])
+def test_elementwise_glue_any_alignment(cuda, nes_lib, oracle_mod, offset, extra):
+    """Depth packing and both quantisers at every input alignment and with
+    element counts that leave a tail after the 4-element vector steps."""
+    torch = cuda
+    lib = nes_lib.load()
+    rng = np.random.default_rng(offset * 7 + extra)
+    n = 4 * 12345 + extra
+    x = np.concatenate([rng.uniform(-0.5, 70.0, n - 6), [np.nan, np.inf, -np.inf, 0.0005, 65.535, -0.0]])
+    x = x.astype(np.float32)
+    src = torch.zeros(n + 8, dtype=torch.float32, device="cuda")
+    src[offset:offset + n] = torch.from_numpy(x).cuda()
+    p = src.data_ptr() + 4 * offset
+    o16 = torch.zeros(n + 8, dtype=torch.int16, device="cuda")
+    nes_lib.depth_pack_u16mm(p, n, o16.data_ptr() + 2 * offset)
+    o8 = torch.zeros(n + 8, dtype=torch.uint8, device="cuda")
+    assert lib.nes_depth_to_gray8(p, n, 4.0, o8.data_ptr() + offset, None) == 0
+    q8 = torch.zeros(n + 8, dtype=torch.uint8, device="cuda")
+    assert lib.nes_rgb_to_rgb24(p, n, q8.data_ptr() + offset, None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(o16.cpu().numpy()[offset:offset + n].view(np.uint16), oracle_mod.depth_pack_u16mm(x))
+    assert np.array_equal(o8.cpu().numpy()[offset:offset + n], oracle_mod.depth_to_gray8(x, 4.0))
+    assert np.array_equal(q8.cpu().numpy()[offset:offset + n], oracle_mod.rgb_to_rgb24(x))
+    # Nothing written outside [offset, offset + n).
+    assert not o16.cpu().numpy()[:offset].any() and not o16.cpu().numpy()[offset + n:].any()
+    assert not o8.cpu().numpy()[offset + n:].any() and not q8.cpu().numpy()[offset + n:].any()

@@ -6,7 +6,11 @@ loss curve and the error paths.
 Tolerances: loss relative 1e-5; gradients (FP32 accumulation with atomics
 in nondeterministic order against FP64) relative L2 error <= 1e-4 per
 parameter block and |delta| <= 1e-3 of the block's largest entry; finite
-differences relative 1e-3."""
+differences relative 1e-3.  The default weight gradients are TF32 tensor-core
+GEMMs (10-bit mantissa operands, FP32 accumulation): their weight blocks are
+held to relative L2 5e-3 and 2e-2 of the largest entry, everything else to
+the FP32 tolerances; `exact_weight_grads=1` (FP32 CUDA cores) is held to the
+FP32 tolerances throughout."""
 import numpy as np
 import pytest
 
@@ -92,16 +96,19 @@ def _close(a, b, rel=1e-4, peak=1e-3):
     return e_rel <= rel and e_peak <= peak
 
 
-def test_gradient_matches_oracle(nes_lib, oracle_mod, setup):
+@pytest.mark.parametrize("exact", [1, 0])
+def test_gradient_matches_oracle(nes_lib, oracle_mod, setup, exact):
     views, rgb, dep = setup
-    r, t = _student(nes_lib, setup)
+    r, t = _student(nes_lib, setup, exact_weight_grads=exact)
+    wrel, wpeak = (1e-4, 1e-3) if exact else (5e-3, 2e-2)
     pairs = _pairs(64, len(views), 3)
     loss, gt, gw = t.grad(pairs, TABLE_FLOATS)
     samples = t.last_samples()
     oloss, ogt, ogw, ocount = _oracle_grad(oracle_mod, r, views, pairs, rgb, dep)
     assert samples == ocount
     assert abs(loss - oloss) <= 1e-5 * oloss
-    bad = [(name, _errs(gw[a:b], ogw[a:b])) for name, (a, b) in BLOCKS.items() if not _close(gw[a:b], ogw[a:b])]
+    bad = [(name, _errs(gw[a:b], ogw[a:b])) for name, (a, b) in BLOCKS.items()
+           if not _close(gw[a:b], ogw[a:b], wrel, wpeak)]
     for lvl in range(16):
         seg = slice(lvl * (1 << LOG2T) * 2, (lvl + 1) * (1 << LOG2T) * 2)
         if not _close(gt[seg], ogt[seg]):
@@ -116,7 +123,7 @@ def test_gradient_matches_oracle(nes_lib, oracle_mod, setup):
 
 def test_gradient_matches_gpu_finite_differences(nes_lib, setup):
     views, rgb, dep = setup
-    r, t = _student(nes_lib, setup)
+    r, t = _student(nes_lib, setup, exact_weight_grads=1)
     pairs = _pairs(128, len(views), 4)
     loss, gt, gw = t.grad(pairs, TABLE_FLOATS)
     l64 = t.loss_fp64(pairs)
@@ -141,6 +148,25 @@ def test_gradient_matches_gpu_finite_differences(nes_lib, setup):
     assert not bad, bad
     t.close()
     r.close()
+
+
+def test_tensor_core_weight_gradients_match_exact(nes_lib, setup):
+    """4,096 rays (~0.9 M samples, ~28 k tiles): every CTA of the TF32 kernel
+    wraps its 3-stage ring many times and ends on a partial tile."""
+    views, rgb, dep = setup
+    pairs = _pairs(4096, len(views), 7)
+    out = {}
+    for exact in (1, 0):
+        r, t = _student(nes_lib, setup, exact_weight_grads=exact)
+        out[exact] = t.grad(pairs, TABLE_FLOATS)
+        t.close()
+        r.close()
+    (l1, gt1, gw1), (l0, gt0, gw0) = out[1], out[0]
+    assert l0 == pytest.approx(l1, rel=1e-6)
+    assert _close(gt0, gt1, 1e-5, 1e-4), _errs(gt0, gt1)
+    bad = [(name, _errs(gw0[a:b], gw1[a:b])) for name, (a, b) in BLOCKS.items()
+           if not _close(gw0[a:b], gw1[a:b], 5e-3, 2e-2)]
+    assert not bad, bad
 
 
 def test_adam_first_step_moves_by_lr(nes_lib, setup):
