@@ -133,20 +133,35 @@ __device__ __forceinline__ uint32_t encode_level(const __half2* __restrict__ tab
   return pk(fmaf(fz, p1.x, gz * p0.x), fmaf(fz, p1.y, gz * p0.y));
 }
 
-// Four levels -> TMEM columns 4C..4C+3 of this lane (no wait).  The store is
-// warp-collective, so every lane executes it; lanes without a sample store
-// zeros.
-template <int C>
-__device__ __forceinline__ void encode_chunk(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
-                                             const float3& x, bool has, uint32_t taddr) {
-  uint32_t a = 0u, b = 0u, c = 0u, d = 0u;
+// All 16 levels -> TMEM columns 0..15 of this lane (no wait).  Every level
+// is computed before the first TMEM store: the stores are compiler
+// barriers, so storing per 4 levels would serialise four rounds of
+// gathers per sample.
+__device__ __forceinline__ void encode_all(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
+                                           const float3& x, bool has, uint32_t taddr) {
+  uint32_t f[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) f[k] = 0u;
   if (has) {
-    a = encode_level<4 * C + 0>(table, T, dense_mask, x);
-    b = encode_level<4 * C + 1>(table, T, dense_mask, x);
-    c = encode_level<4 * C + 2>(table, T, dense_mask, x);
-    d = encode_level<4 * C + 3>(table, T, dense_mask, x);
+    f[0] = encode_level<0>(table, T, dense_mask, x);
+    f[1] = encode_level<1>(table, T, dense_mask, x);
+    f[2] = encode_level<2>(table, T, dense_mask, x);
+    f[3] = encode_level<3>(table, T, dense_mask, x);
+    f[4] = encode_level<4>(table, T, dense_mask, x);
+    f[5] = encode_level<5>(table, T, dense_mask, x);
+    f[6] = encode_level<6>(table, T, dense_mask, x);
+    f[7] = encode_level<7>(table, T, dense_mask, x);
+    f[8] = encode_level<8>(table, T, dense_mask, x);
+    f[9] = encode_level<9>(table, T, dense_mask, x);
+    f[10] = encode_level<10>(table, T, dense_mask, x);
+    f[11] = encode_level<11>(table, T, dense_mask, x);
+    f[12] = encode_level<12>(table, T, dense_mask, x);
+    f[13] = encode_level<13>(table, T, dense_mask, x);
+    f[14] = encode_level<14>(table, T, dense_mask, x);
+    f[15] = encode_level<15>(table, T, dense_mask, x);
   }
-  tc::tmem_st4(taddr + 4 * C, a, b, c, d);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) tc::tmem_st4(taddr + 4 * c, f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]);
 }
 
 // D[128 x N] = A[128 x K] (TMEM) * B[N x K]^T (shared), K in steps of 16
@@ -386,10 +401,7 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
       uint32_t tag = 0;
       const float t = has ? fmaf((float)q.ei + 0.5f, kDt, q.ts) : 0.0f;
       const float3 x = sample_pos(q.o, q.d, t);
-      encode_chunk<0>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
-      encode_chunk<1>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
-      encode_chunk<2>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
-      encode_chunk<3>(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
+      encode_all(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
       if (has) {
         dirs[b * 128 + row] = make_float4(q.d.x, q.d.y, q.d.z, 0.0f);
         tag = 1u | ((uint32_t)q.ec << 1);
