@@ -15,22 +15,27 @@
 // One CTA per SM: 4 groups x (4 ENCODER warps + 4 MLP warps) = 1024 threads.
 //  - ENCODER thread = one ray slot.  Per tile it claims rays (a warp-wide
 //    chunk of 32 at a time), encodes its slot's next occupied sample from the
-//    FP16 table (FP32 interpolation), writes the 32 FP16 features as its
-//    TMEM lane of the tile (16 columns) and marks the tile full.  Encoders run
-//    one tile ahead of the MLP (two tile buffers), then composite the
-//    previous tile's results (FP32 transmittance, colour, depth).
+//    FP16 table, writes the 32 FP16 features as its TMEM lane of the tile (16
+//    columns), hands the row's ray id, flags, direction and t over in shared
+//    memory and marks the tile full.  It never waits for results: only for
+//    its tile buffer to be free again (two buffers), which the MLP's first
+//    layer releases through its MMA commit.  Encoder warps run independently.
 //  - MLP thread = TMEM lane = tile row.  One thread issues each layer
 //    (32->64, 64->16, 32->64, 64->64, 64->16 [3 used]) as tcgen05.mma
 //    kind::f16 with A from TMEM and B from shared memory, FP32 accumulators in
 //    TMEM; between layers every thread loads its lane, applies ReLU / exp and
-//    stores the next FP16 A operand back to TMEM.
-//  - A sample encoded speculatively for a ray that terminates early
-//    (T < 1e-4) is discarded at compositing time.
+//    stores the next FP16 A operand back to TMEM.  The same thread then
+//    composites its row's sample into the row's ray (FP32 transmittance,
+//    colour, depth): a row's samples arrive in order, so each ray is
+//    composited by one thread with one state.
+//  - Early termination (T < 1e-4) is noticed by the MLP thread, which writes
+//    the ray and tells the row's encoder to move on; samples the encoder
+//    produced meanwhile are dropped.
 // TMEM (512 columns): group g encoder tiles at 32g (+16 for the second
-// buffer), MLP hidden activations at 128+96g (32 columns of packed FP16),
-// accumulator after them (64 FP32 columns).  Two CTAs cannot share an SM:
-// 1024 threads x >32 registers fill the register file, and the launcher
-// checks it.
+// buffer), MLP hidden activations at 128+96g (32 columns of packed FP16;
+// also the colour input), accumulator after them (64 FP32 columns).  Two CTAs
+// cannot share an SM: 1024 threads x >32 registers fill the register file,
+// and the launcher checks it.
 #include <cuda_fp16.h>
 
 #include "kernels.h"
@@ -44,7 +49,7 @@ constexpr int kGroups = 4;
 constexpr int kRoleThreads = 128;  // encoder threads = MLP threads = tile rows
 constexpr int kGroupThreads = 2 * kRoleThreads;
 constexpr int kTcThreads = kGroups * kGroupThreads;  // 1024
-constexpr uint32_t kLaunchRegs = 64, kEncRegs = 80, kMlpRegs = 48;
+constexpr uint32_t kLaunchRegs = 64, kEncRegs = 72, kMlpRegs = 56;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kEncColsPerGroup = 32;  // two 16-column tile buffers
 constexpr uint32_t kMlpBase = kGroups * kEncColsPerGroup;
@@ -59,12 +64,15 @@ constexpr int kWoffCW2 = 10240;  // N=64, K=64
 constexpr int kWoffCW3 = 18432;  // N=16 (rows 3..15 zero), K=64
 constexpr int kWBytes = 20480;
 
-// Per-group shared memory: per-row ray directions and results for both tile
-// buffers, stop flags and mbarriers.
-constexpr int kGOffDir = 0;                         // [2][128] float4 (d, unused)
-constexpr int kGOffRes = kGOffDir + 2 * 128 * 16;   // [2][128] float4 (sigma, r, g, b)
-constexpr int kGOffStop = kGOffRes + 2 * 128 * 16;  // [2] uint32
-constexpr int kGOffBar = kGOffStop + 16;            // full0, full1, done0, done1, mma
+// Per-group shared memory: per-row hand-off (direction + t, ray id + flags)
+// for both tile buffers, per-warp "out of rays" flags, early-termination
+// notices, the group's stop flag and mbarriers.
+constexpr int kGOffInfo = 0;                          // [2][128] float4 (d, t)
+constexpr int kGOffTag = kGOffInfo + 2 * 128 * 16;    // [2][128] uint2 (ray id, flags)
+constexpr int kGOffFin = kGOffTag + 2 * 128 * 8;      // [2][4] uint32
+constexpr int kGOffTerm = kGOffFin + 32;              // [128] uint32
+constexpr int kGOffDone = kGOffTerm + 128 * 4;        // uint32
+constexpr int kGOffBar = (kGOffDone + 4 + 7) / 8 * 8; // full0, full1, free0, free1, mma
 constexpr int kGroupBytes = (kGOffBar + 5 * 8 + 127) / 128 * 128;
 
 constexpr int kOffW = 0;
@@ -171,16 +179,17 @@ __device__ __forceinline__ void mma_layer(uint32_t d_tmem, uint32_t a_tmem, uint
     tc::mma_f16_at(d_tmem, a_tmem + j * 8, tc::sdesc(b + j * 256, 128, K * 16), idesc, j > 0 ? 1u : 0u);
 }
 
-// 64 accumulator columns -> ReLU -> FP16 -> 32 hidden-activation columns.
+// 64 accumulator columns -> ReLU -> FP16 -> 32 hidden-activation columns, in
+// four 16-column slices so that few registers are live at once.
 __device__ __forceinline__ void relu_to_h(uint32_t d_row, uint32_t h_row) {
 #pragma unroll
-  for (int half = 0; half < 2; ++half) {
-    float v[32];
-    tc::tmem_ld32(d_row + 32 * half, v);
-    uint32_t w[16];
+  for (int q = 0; q < 4; ++q) {
+    float v[16];
+    tc::tmem_ld16(d_row + 16 * q, v);
+    uint32_t w[8];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) w[k] = pk_relu(v[2 * k], v[2 * k + 1]);
-    tc::tmem_st16(h_row + 16 * half, w);
+    for (int k = 0; k < 8; ++k) w[k] = pk_relu(v[2 * k], v[2 * k + 1]);
+    tc::tmem_st8(h_row + 8 * q, w);
   }
 }
 
@@ -196,20 +205,17 @@ __device__ __forceinline__ void write_ray(const ViewBatch& vb, const DevScratch&
   if (V.depth) V.depth[m.pixel] = dep;
 }
 
-// Encoder-side state of one ray slot.  Two compositing contexts: the ray
-// being encoded and, for one tile after a ray switch, the previous ray.
+// Per-row hand-off flags of a tile (with the ray id, encoder -> MLP).
+constexpr uint32_t kTagSample = 1u, kTagFirst = 2u, kTagLast = 4u;
+
+// Encoder-side state of one ray slot.
 struct Slot {
-  bool enc_live = false;
-  int ec = 1;  // context of the ray being encoded (the first ray gets 0)
+  bool live = false;
+  bool first = false;
   float3 o, d;
   float ts = 0.0f;
   int n = 0, ei = 0;
-  uint32_t id0 = 0, id1 = 0;
-  float T0 = 1.0f, r0 = 0.0f, g0 = 0.0f, b0 = 0.0f, z0 = 0.0f;
-  float T1 = 1.0f, r1 = 0.0f, g1 = 0.0f, b1 = 0.0f, z1 = 0.0f;
-  uint32_t live = 0;      // bit c: context c still accumulating
-  uint32_t tag0 = 0, tag1 = 0;  // per buffer: bit0 sample, bit1 context, bit2 last sample of its ray
-  float t0 = 0.0f, t1 = 0.0f;
+  uint32_t id = 0;
 };
 
 __device__ __forceinline__ void skip_empty(const DevScene& sc, Slot& q) {
@@ -225,23 +231,31 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
   const bool is_mlp = (tid % kGroupThreads) >= kRoleThreads;
   const int row = tid % kRoleThreads;  // tile row = TMEM lane
   uint8_t* G = smem + kOffGroups + g * kGroupBytes;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(G + kGOffBar);  // full0, full1, done0, done1, mma
-  uint32_t* stop = reinterpret_cast<uint32_t*>(G + kGOffStop);
-  float4* dirs = reinterpret_cast<float4*>(G + kGOffDir);
-  float4* res = reinterpret_cast<float4*>(G + kGOffRes);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(G + kGOffBar);  // full0, full1, free0, free1, mma
+  float4* info = reinterpret_cast<float4*>(G + kGOffInfo);    // [2][128] (d, t)
+  uint2* tagw = reinterpret_cast<uint2*>(G + kGOffTag);       // [2][128] (ray id, flags)
+  uint32_t* wfin = reinterpret_cast<uint32_t*>(G + kGOffFin); // [2][4] encoder warp finished
+  uint32_t* term = reinterpret_cast<uint32_t*>(G + kGOffTerm);  // [128] early-terminated ray id + 1
+  volatile uint32_t* gdone = reinterpret_cast<volatile uint32_t*>(G + kGOffDone);
   uint64_t* bar_w = reinterpret_cast<uint64_t*>(smem + kOffBarW);
   uint32_t* slot = reinterpret_cast<uint32_t*>(smem + kOffSlot);
-  const uint32_t enc_bar = 1 + 2 * g, mlp_bar = 2 + 2 * g;
+  const uint32_t mlp_bar = 1 + g;
 
   if (tid == 0) {
     tc::mbar_init(bar_w, 1);
     for (int k = 0; k < kGroups; ++k) {
-      uint64_t* b = reinterpret_cast<uint64_t*>(smem + kOffGroups + k * kGroupBytes + kGOffBar);
-      for (int j = 0; j < 4; ++j) tc::mbar_init(b + j, kRoleThreads);
-      tc::mbar_init(b + 4, 1);
+      uint8_t* Gk = smem + kOffGroups + k * kGroupBytes;
+      uint64_t* b = reinterpret_cast<uint64_t*>(Gk + kGOffBar);
+      tc::mbar_init(b + 0, kRoleThreads);  // full: every encoder thread arrives
+      tc::mbar_init(b + 1, kRoleThreads);
+      tc::mbar_init(b + 2, 1);             // free: the layer-1 commit (or the stop) arrives
+      tc::mbar_init(b + 3, 1);
+      tc::mbar_init(b + 4, 1);             // mma: commit of each layer
+      *reinterpret_cast<uint32_t*>(Gk + kGOffDone) = 0u;
     }
     tc::fence_mbar_init();
   }
+  if (!is_mlp) term[row] = 0u;
   if (warp == 0) {
     tc::tmem_alloc(slot, kTmemCols);
     tc::tmem_relinquish();
@@ -261,109 +275,150 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
   fail = __syncthreads_or(fail);
 
   // Registers move from the MLP warpgroups to the gather-bound encoders:
-  // 512 x 80 + 512 x 48 = 1024 x 64, the launch allocation.
-  // Each role sets its budget first thing in its own branch (fail is
-  // CTA-uniform, so a warpgroup either runs its branch whole or not at all).
+  // 512 x kEncRegs + 512 x kMlpRegs = 1024 x 64, the launch allocation
+  // (the launcher checks the kernel was built with exactly 64).
   static_assert(kGroups * kRoleThreads * (kEncRegs + kMlpRegs) == kTcThreads * kLaunchRegs, "register split");
 
   unsigned long long my_samples = 0;
   if (!fail && is_mlp) {
     // ======================= MLP warps =======================
+    // One thread per tile row: it evaluates the row's sample through the
+    // five layers and composites it into the row's current ray, so a ray's
+    // samples are composited in order by one thread with one state.
     tc::regs_dec<kMlpRegs>();
     const uint32_t sW = tc::smem_addr(smem + kOffW);
     const uint32_t h_col = tmem + kMlpBase + g * kMlpColsPerGroup;  // hidden activations (lane 0)
     const uint32_t d_col = h_col + 32;                              // accumulator (lane 0)
     const uint32_t d_row = d_col + lane_off, h_row = h_col + lane_off;
     constexpr uint32_t id64 = tc::idesc_f16_f32(128, 64), id16 = tc::idesc_f16_f32(128, 16);
-    uint32_t pf0 = 0, pf1 = 0, pm = 0;
+    uint32_t pm = 0;
+    uint32_t cur = 0xFFFFFFFFu;  // ray being composited in this row (none)
+    float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f, cz = 0.0f;
 
-    // One layer: publish this thread's TMEM writes, one thread issues and
-    // waits, the warps learn the outcome.
-    auto layer = [&](uint32_t a_tmem, uint32_t b_off, int K, uint32_t idesc, bool publish) -> bool {
-      if (publish) {
-        tc::fence_before();
-        tc::named_sync(mlp_bar, kRoleThreads);
-      }
-      bool bad = false;
+    // Issues one layer (one thread) and waits for it (every thread); the
+    // free barrier of the tile's buffer, if given, is released by the same
+    // completion.
+    auto layer = [&](uint32_t a_tmem, uint32_t b_off, int K, uint32_t idesc, uint64_t* also) -> bool {
       if (row == 0) {
         tc::fence_after();
         mma_layer(d_col, a_tmem, sW + b_off, K, idesc);
         tc::mma_commit(bar + 4);
-        bad = !tc::mbar_wait_sleep(bar + 4, pm);
+        if (also) tc::mma_commit(also);
       }
+      const bool ok = tc::mbar_wait(bar + 4, pm);
       pm ^= 1u;
-      bad = tc::named_sync_or(mlp_bar, kRoleThreads, bad);
       tc::fence_after();
-      return !bad;
+      return ok;
+    };
+    // This thread's TMEM writes -> visible to the next MMA.
+    auto publish = [&]() {
+      tc::fence_before();
+      tc::named_sync(mlp_bar, kRoleThreads);
     };
 
-    auto run_tile = [&](int b, uint32_t& pf) -> int {  // 1 processed, 0 stop, -1 failure
-      bool bad = false, st = false;
-      if (row == 0) {
-        bad = !tc::mbar_wait_sleep(bar + b, pf);
-        st = bad || stop[b] != 0;
+    for (uint32_t k = 0;; ++k) {
+      const int b = (int)(k & 1u);
+      if (!tc::mbar_wait_sleep(bar + b, (k >> 1) & 1u)) { fail = true; break; }
+      tc::fence_after();
+      if (wfin[b * 4 + 0] & wfin[b * 4 + 1] & wfin[b * 4 + 2] & wfin[b * 4 + 3]) {
+        // Every encoder warp of the group is out of rays: release the
+        // encoders that wait for this buffer and stop.
+        if (row == 0) {
+          *gdone = 1u;
+          tc::mbar_arrive(bar + 2 + b);
+        }
+        break;
       }
-      pf ^= 1u;
-      if (tc::named_sync_or(mlp_bar, kRoleThreads, bad)) return -1;
-      if (tc::named_sync_or(mlp_bar, kRoleThreads, st)) return 0;
-      const uint32_t a_col = enc_cols + 16 * b;  // encoded features, later the colour input
-      // density 32 -> 64 -> 16
-      if (!layer(a_col, kWoffDW1, 32, id64, false)) return -1;
+      const uint2 tg = tagw[b * 128 + row];
+      const float4 di = info[b * 128 + row];
+      const uint32_t a_col = enc_cols + 16 * b;  // encoded features of this tile
+      // density 32 -> 64 -> 16 (the first layer is the features' last reader)
+      if (!layer(a_col, kWoffDW1, 32, id64, bar + 2 + b)) { fail = true; break; }
       relu_to_h(d_row, h_row);
-      if (!layer(h_col, kWoffDW2, 64, id16, true)) return -1;
+      publish();
+      if (!layer(h_col, kWoffDW2, 64, id16, nullptr)) { fail = true; break; }
       float sigma;
       {
+        // colour input [SH16(d) | density outputs 1..15 | 0] -> h (layer 2
+        // is done with h)
         float v[16];
         tc::tmem_ld16(d_row, v);
         sigma = expf(v[0] - 1.0f);
-        const float4 dd = dirs[b * 128 + row];
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 7; ++j) w[j] = pk(v[1 + 2 * j], v[2 + 2 * j]);
+        w[7] = pk(v[15], 0.0f);
+        tc::tmem_st8(h_row + 8, w);
         float sh[16];
-        sh16(make_float3(dd.x, dd.y, dd.z), sh);
-        uint32_t w[16];
+        sh16(make_float3(di.x, di.y, di.z), sh);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) w[k] = pk(sh[2 * k], sh[2 * k + 1]);
-#pragma unroll
-        for (int k = 0; k < 7; ++k) w[8 + k] = pk(v[1 + 2 * k], v[2 + 2 * k]);
-        w[15] = pk(v[15], 0.0f);
-        tc::tmem_st16(a_col + lane_off, w);  // layer 1 is done with this buffer
+        for (int j = 0; j < 8; ++j) w[j] = pk(sh[2 * j], sh[2 * j + 1]);
+        tc::tmem_st8(h_row, w);
       }
+      publish();
       // colour 32 -> 64 -> 64 -> 3
-      if (!layer(a_col, kWoffCW1, 32, id64, true)) return -1;
+      if (!layer(h_col, kWoffCW1, 32, id64, nullptr)) { fail = true; break; }
       relu_to_h(d_row, h_row);
-      if (!layer(h_col, kWoffCW2, 64, id64, true)) return -1;
+      publish();
+      if (!layer(h_col, kWoffCW2, 64, id64, nullptr)) { fail = true; break; }
       relu_to_h(d_row, h_row);
-      if (!layer(h_col, kWoffCW3, 64, id16, true)) return -1;
+      publish();
+      if (!layer(h_col, kWoffCW3, 64, id16, nullptr)) { fail = true; break; }
       float v5[16];
       tc::tmem_ld16(d_row, v5);
-      tc::fence_before();
-      res[b * 128 + row] = make_float4(sigma, sigmoidf(v5[0]), sigmoidf(v5[1]), sigmoidf(v5[2]));
-      tc::mbar_arrive(bar + 2 + b);
-      return 1;
-    };
-
-    for (;;) {
-      int rc = run_tile(0, pf0);
-      if (rc <= 0) { fail = rc < 0; break; }
-      rc = run_tile(1, pf1);
-      if (rc <= 0) { fail = rc < 0; break; }
+      // Compositing (FP32, every operation rounded explicitly).
+      if (tg.y & kTagSample) {
+        if (tg.y & kTagFirst) {
+          cur = tg.x;
+          T = 1.0f;
+          cr = cg = cb = cz = 0.0f;
+        }
+        if (cur == tg.x) {  // samples of a ray that already terminated are dropped
+          ++my_samples;
+          const float alpha = -expm1f(__fmul_rn(-sigma, kDt));
+          const float wgt = __fmul_rn(T, alpha);
+          cr = __fmaf_rn(wgt, sigmoidf(v5[0]), cr);
+          cg = __fmaf_rn(wgt, sigmoidf(v5[1]), cg);
+          cb = __fmaf_rn(wgt, sigmoidf(v5[2]), cb);
+          cz = __fmaf_rn(wgt, di.w, cz);
+          T = __fsub_rn(T, wgt);
+          const bool stop_early = T < kTStop;
+          if (stop_early || (tg.y & kTagLast)) {
+            write_ray(vb, s, cur, cr, cg, cb, cz);
+            if (stop_early && !(tg.y & kTagLast)) term[row] = cur + 1u;  // tells the encoder to move on
+            cur = 0xFFFFFFFFu;
+          }
+        }
+      }
+      // The next tile's first layer overwrites the accumulator this thread
+      // has just read.
+      publish();
     }
   } else if (!fail) {
     // ======================= encoder warps =======================
+    // Each warp runs on its own: it waits only for its tile buffer to be
+    // free (the MLP's first layer has read it), never for results.
     tc::regs_inc<kEncRegs>();
     const uint32_t nrays = min(s.counters[kCtrRays], s.max_rays);
+    const int wq = warp & 3;
     Slot q;
-    uint32_t pd0 = 0, pd1 = 0;
     bool exhausted = false;
-
-    // Encodes the slot's next sample into buffer b and marks it full.
-    // Returns whether any slot of the group had a sample.
-    auto encode_step = [&](int b) -> bool {
+    for (uint32_t k = 0;; ++k) {
+      const int b = (int)(k & 1u);
+      if (k >= 2) {
+        bool ok = true;
+        if (lane == 0) ok = tc::mbar_wait_sleep(bar + 2 + b, ((k >> 1) - 1u) & 1u);
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (!ok) { fail = true; break; }
+        if (*gdone) break;
+      }
+      // A ray the MLP terminated early (T < 1e-4) is encoded no further.
+      if (q.live && term[row] == q.id + 1u) q.live = false;
       // Refill a whole warp at once: the warp claims 32 consecutive rays (one
       // 4x8 pixel tile) only when all its lanes are done, so its 32 samples
-      // stay neighbours in space and each warp-wide gather stays coherent
-      // (lanes refilled one by one drift apart and gather ~2.5x slower).
+      // stay neighbours in space and each warp-wide gather stays coherent.
       for (;;) {
-        if (__ballot_sync(0xffffffffu, q.enc_live) != 0u || exhausted) break;
+        if (__ballot_sync(0xffffffffu, q.live) != 0u || exhausted) break;
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(s.counters + kCtrCursor, 32u);
         base = __shfl_sync(0xffffffffu, base, 0);
@@ -381,92 +436,42 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
           q.ts = rd.w;
           q.n = m.n;
           q.ei = 0;
+          q.id = id;
           skip_empty(sc, q);
           if (q.ei < q.n) {
-            q.enc_live = true;
-            q.ec ^= 1;
-            if (q.ec == 0) {
-              q.id0 = id; q.T0 = 1.0f; q.r0 = q.g0 = q.b0 = q.z0 = 0.0f;
-            } else {
-              q.id1 = id; q.T1 = 1.0f; q.r1 = q.g1 = q.b1 = q.z1 = 0.0f;
-            }
-            q.live |= 1u << q.ec;
+            q.live = true;
+            q.first = true;
           } else {
             write_ray(vb, s, id, 0.0f, 0.0f, 0.0f, 0.0f);  // no occupied sample
           }
         }
       }
-      const uint32_t a_row = enc_cols + 16 * b + lane_off;
-      const bool has = q.enc_live;
+      const bool has = q.live;
       uint32_t tag = 0;
       const float t = has ? fmaf((float)q.ei + 0.5f, kDt, q.ts) : 0.0f;
       const float3 x = sample_pos(q.o, q.d, t);
-      encode_all(sc.table16, sc.T, sc.dense_mask, x, has, a_row);
+      encode_all(sc.table16, sc.T, sc.dense_mask, x, has, enc_cols + 16 * b + lane_off);
       if (has) {
-        dirs[b * 128 + row] = make_float4(q.d.x, q.d.y, q.d.z, 0.0f);
-        tag = 1u | ((uint32_t)q.ec << 1);
+        tag = kTagSample | (q.first ? kTagFirst : 0u);
+        q.first = false;
         ++q.ei;
         skip_empty(sc, q);
         if (q.ei >= q.n) {
-          tag |= 4u;
-          q.enc_live = false;
+          tag |= kTagLast;
+          q.live = false;
         }
-      } else {
-        dirs[b * 128 + row] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
       }
-      if (b == 0) { q.tag0 = tag; q.t0 = t; } else { q.tag1 = tag; q.t1 = t; }
+      info[b * 128 + row] = make_float4(q.d.x, q.d.y, q.d.z, t);
+      tagw[b * 128 + row] = make_uint2(q.id, tag);
+      const bool fin = exhausted && __ballot_sync(0xffffffffu, has) == 0u;
+      if (lane == 0) wfin[b * 4 + wq] = fin ? 1u : 0u;
       tc::tmem_wait_st();
       tc::fence_before();
-      const bool any = tc::named_sync_or(enc_bar, kRoleThreads, has);
-      if (row == 0) stop[b] = any ? 0u : 1u;
       tc::mbar_arrive(bar + b);
-      return any;
-    };
-
-    // Waits for buffer b's results and composites them.  False on timeout.
-    auto composite_step = [&](int b, uint32_t& pd) -> bool {
-      bool bad = false;
-      if (row == 0) bad = !tc::mbar_wait_sleep(bar + 2 + b, pd);
-      pd ^= 1u;
-      if (tc::named_sync_or(enc_bar, kRoleThreads, bad)) return false;
-      const uint32_t tag = b == 0 ? q.tag0 : q.tag1;
-      if (!(tag & 1u)) return true;
-      const int c = (tag >> 1) & 1;
-      if (!((q.live >> c) & 1u)) return true;  // ray already finished: discard the speculative sample
-      const float4 v = res[b * 128 + row];
-      const float t = b == 0 ? q.t0 : q.t1;
-      ++my_samples;
-      const float alpha = -expm1f(-v.x * kDt);
-      float& T = c == 0 ? q.T0 : q.T1;
-      float& cr = c == 0 ? q.r0 : q.r1;
-      float& cg = c == 0 ? q.g0 : q.g1;
-      float& cb = c == 0 ? q.b0 : q.b1;
-      float& z = c == 0 ? q.z0 : q.z1;
-      const float wgt = T * alpha;
-      cr = fmaf(wgt, v.y, cr);
-      cg = fmaf(wgt, v.z, cg);
-      cb = fmaf(wgt, v.w, cb);
-      z = fmaf(wgt, t, z);
-      T -= wgt;
-      if (T < kTStop || (tag & 4u)) {
-        write_ray(vb, s, c == 0 ? q.id0 : q.id1, cr, cg, cb, z);
-        q.live &= ~(1u << c);
-        if (c == q.ec) q.enc_live = false;  // early termination: stop encoding this ray
-      }
-      return true;
-    };
-
-    bool more = encode_step(0);
-    while (more) {
-      const bool more1 = encode_step(1);
-      if (!composite_step(0, pd0)) { fail = true; break; }
-      if (!more1) break;
-      more = encode_step(0);
-      if (!composite_step(1, pd1)) { fail = true; break; }
     }
   }
 
-  if (fail && (tid % kRoleThreads) == 0) atomicExch(s.counters + kCtrError, 1u);
+  if (fail) atomicExch(s.counters + kCtrError, 1u);
   tc::fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -527,7 +532,9 @@ cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const
   cudaFuncAttributes fa;
   cudaError_t e = cudaFuncGetAttributes(&fa, march_tc_kernel);
   if (e != cudaSuccess) return e;
-  if (fa.numRegs <= 32) return cudaErrorInvalidConfiguration;
+  // The setmaxnreg split hands out exactly 1024 x kLaunchRegs registers: a
+  // build with a smaller launch allocation would stall the encoders' increase.
+  if (fa.numRegs != (int)kLaunchRegs) return cudaErrorInvalidConfiguration;
   march_tc_kernel<<<num_sms, kTcThreads, kSmemRequest, stream>>>(views, scene, s);
   return cudaGetLastError();
 }

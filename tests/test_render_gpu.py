@@ -77,6 +77,19 @@ def test_batched_views_equal_single_views(renderer, cuda, nes_lib):
         assert np.array_equal(rgb, rgb1) and np.array_equal(dep, dep1)
 
 
+def test_views_behind_a_large_view_equal_single_views(renderer, cuda, nes_lib):
+    """A 1280x720 view first gives every march slot several rays, so the small
+    views behind it run in slots with a history (the tensor-core march keeps
+    two compositing contexts per slot); their pixels must not change."""
+    poses = nes_lib.shell_poses(12, 4, 1.2, 2.0)
+    small = [(m, 96, 64, nes_lib.focal_from_fov(96, 100.0)) for m in nes_lib.stereo_pair(poses[3], 0.063)]
+    views = [(poses[1], 1280, 720, nes_lib.focal_from_fov(1280, 90.0))] + small
+    batched = render_gpu(renderer, cuda, views)
+    for v, (rgb, dep) in zip(small, batched[1:]):
+        (rgb1, dep1), = render_gpu(renderer, cuda, [v])
+        assert np.array_equal(rgb, rgb1) and np.array_equal(dep, dep1)
+
+
 def test_stereo_pair_vs_oracle(renderer, cuda, scene0, nes_lib):
     pose = nes_lib.shell_poses(2, 1, 1.2, 2.0)[0]
     W, H = 40, 38
