@@ -20,6 +20,7 @@ struct nes_ctx {
 
   float2* d_table32 = nullptr;
   __half2* d_table16 = nullptr;
+  uint4* d_rec16 = nullptr;
   float* d_weights = nullptr;
   uint8_t* d_tc_weights = nullptr;
   uint32_t* d_occ = nullptr;

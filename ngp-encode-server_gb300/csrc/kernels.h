@@ -15,6 +15,7 @@ namespace nes {
 struct DevScene {
   const float2* table32 = nullptr;  // [16][T] float2
   const __half2* table16 = nullptr; // [16][T] half2 (tensor-core path)
+  const uint4* rec16 = nullptr;     // per-cell corner records of levels 0..kRecLevels-1 (2 x uint4 each)
   const float* weights = nullptr;   // kWeightFloats FP32 blob
   const uint8_t* tc_weights = nullptr; // FP16 weights in the MMA operand layout
   const uint32_t* occ = nullptr;    // kOccWords
@@ -50,6 +51,12 @@ cudaError_t launch_march_fp32(const ViewBatch& views, const DevScene& scene, con
 // scene.tc_weights (the FP16 operand image from launch_pack_tc_weights).
 cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
                             int num_sms, cudaStream_t stream);
+
+// Bytes of the per-cell corner records and their construction from the FP16
+// table (tensor-core path).
+size_t tc_record_bytes();
+cudaError_t launch_build_records(const __half2* table16, uint32_t T, uint32_t dense_mask, uint4* rec,
+                                 cudaStream_t stream);
 
 // Bytes of the FP16 MLP weight image and its packing from the FP32 blob.
 size_t tc_weight_bytes();

@@ -49,7 +49,7 @@ constexpr int kGroups = 4;
 constexpr int kRoleThreads = 128;  // encoder threads = MLP threads = tile rows
 constexpr int kGroupThreads = 2 * kRoleThreads;
 constexpr int kTcThreads = kGroups * kGroupThreads;  // 1024
-constexpr uint32_t kLaunchRegs = 64, kEncRegs = 72, kMlpRegs = 56;
+constexpr uint32_t kLaunchRegs = 64, kEncRegs = 80, kMlpRegs = 48;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kEncColsPerGroup = 32;  // two 16-column tile buffers
 constexpr uint32_t kMlpBase = kGroups * kEncColsPerGroup;
@@ -91,7 +91,32 @@ __host__ __device__ constexpr int op_chunk(int n, int c, int K) { return (n >> 3
 
 __device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
 __device__ __forceinline__ uint32_t pk(float a, float b) { return h2u(__floats2half2_rn(a, b)); }
-__device__ __forceinline__ uint32_t pk_relu(float a, float b) { return pk(fmaxf(a, 0.0f), fmaxf(b, 0.0f)); }
+// max(a, 0), max(b, 0) -> packed FP16 (a in the low half), one instruction.
+__device__ __forceinline__ uint32_t pk_relu(float a, float b) {
+  uint32_t r;
+  asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  return r;
+}
+
+// Trilinear interpolation of 8 FP16 corner entries (corner c = dx + 2 dy +
+// 4 dz): per z-plane bilinear partial sums in packed HFMA2 with weights
+// rounded to FP16 (|sum| <= 0.5, adding ~1e-4 error, the size of the table's
+// own FP16 rounding), the final z-interpolation in FP32.
+__device__ __forceinline__ uint32_t interp_packed(const __half2 (&e)[8], float fx, float fy, float fz) {
+  const float gx = 1.0f - fx, gy = 1.0f - fy;
+  const __half2 w0 = __float2half2_rn(gx * gy), w1 = __float2half2_rn(fx * gy);
+  const __half2 w2 = __float2half2_rn(gx * fy), w3 = __float2half2_rn(fx * fy);
+  __half2 s0 = __hmul2(w0, e[0]), s1 = __hmul2(w0, e[4]);
+  s0 = __hfma2(w1, e[1], s0);
+  s1 = __hfma2(w1, e[5], s1);
+  s0 = __hfma2(w2, e[2], s0);
+  s1 = __hfma2(w2, e[6], s1);
+  s0 = __hfma2(w3, e[3], s0);
+  s1 = __hfma2(w3, e[7], s1);
+  const float2 p0 = __half22float2(s0), p1 = __half22float2(s1);
+  const float gz = 1.0f - fz;
+  return pk(fmaf(fz, p1.x, gz * p0.x), fmaf(fz, p1.y, gz * p0.y));
+}
 
 // Level L of the FP16 table at x -> its two features packed as FP16.
 // Instruction-lean form of the trilinear interpolation (the march is
@@ -100,6 +125,32 @@ __device__ __forceinline__ uint32_t pk_relu(float a, float b) { return pk(fmaxf(
 // partial sums of the FP16 entries with packed HFMA2 (weights rounded to
 // FP16, |sum| <= 0.5, adding ~1e-4 error, the size of the table's own FP16
 // rounding); the final z-interpolation is FP32.
+// Levels 0..kRecLevels-1 also exist as per-cell records: the 8 corner
+// entries of every cell (c = dx + 2 dy + 4 dz) in 32 contiguous bytes, so a
+// sample's level costs two 16-byte loads instead of eight scattered 4-byte
+// gathers (the encoder is bound by L1 wavefronts).  The records are copies of
+// table entries (built by build_records_kernel), so the result is the same.
+template <int L>
+__device__ __forceinline__ uint32_t encode_level_rec(const uint4* __restrict__ rec, const float3& x) {
+  constexpr int N = level_res(L);
+  const float px = x.x * (float)N, py = x.y * (float)N, pz = x.z * (float)N;
+  const int ix = min(__float2int_rd(px), N - 1), iy = min(__float2int_rd(py), N - 1),
+            iz = min(__float2int_rd(pz), N - 1);
+  const float fx = px - (float)ix, fy = py - (float)iy, fz = pz - (float)iz;
+  const uint32_t cell = rec_cell_offset(L) + (uint32_t)ix + (uint32_t)N * ((uint32_t)iy + (uint32_t)N * (uint32_t)iz);
+  const uint4 a = __ldg(rec + 2 * cell), b = __ldg(rec + 2 * cell + 1);
+  __half2 e[8];
+  e[0] = *reinterpret_cast<const __half2*>(&a.x);
+  e[1] = *reinterpret_cast<const __half2*>(&a.y);
+  e[2] = *reinterpret_cast<const __half2*>(&a.z);
+  e[3] = *reinterpret_cast<const __half2*>(&a.w);
+  e[4] = *reinterpret_cast<const __half2*>(&b.x);
+  e[5] = *reinterpret_cast<const __half2*>(&b.y);
+  e[6] = *reinterpret_cast<const __half2*>(&b.z);
+  e[7] = *reinterpret_cast<const __half2*>(&b.w);
+  return interp_packed(e, fx, fy, fz);
+}
+
 template <int L>
 __device__ __forceinline__ uint32_t encode_level(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
                                                  const float3& x) {
@@ -126,38 +177,28 @@ __device__ __forceinline__ uint32_t encode_level(const __half2* __restrict__ tab
   __half2 e[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) e[k] = __ldg(tab + idx[k]);
-  const float gx = 1.0f - fx, gy = 1.0f - fy;
-  const __half2 w0 = __float2half2_rn(gx * gy), w1 = __float2half2_rn(fx * gy);
-  const __half2 w2 = __float2half2_rn(gx * fy), w3 = __float2half2_rn(fx * fy);
-  __half2 s0 = __hmul2(w0, e[0]), s1 = __hmul2(w0, e[4]);
-  s0 = __hfma2(w1, e[1], s0);
-  s1 = __hfma2(w1, e[5], s1);
-  s0 = __hfma2(w2, e[2], s0);
-  s1 = __hfma2(w2, e[6], s1);
-  s0 = __hfma2(w3, e[3], s0);
-  s1 = __hfma2(w3, e[7], s1);
-  const float2 p0 = __half22float2(s0), p1 = __half22float2(s1);
-  const float gz = 1.0f - fz;
-  return pk(fmaf(fz, p1.x, gz * p0.x), fmaf(fz, p1.y, gz * p0.y));
+  return interp_packed(e, fx, fy, fz);
 }
 
 // All 16 levels -> TMEM columns 0..15 of this lane (no wait).  Every level
 // is computed before the first TMEM store: the stores are compiler
 // barriers, so storing per 4 levels would serialise four rounds of
 // gathers per sample.
-__device__ __forceinline__ void encode_all(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
-                                           const float3& x, bool has, uint32_t taddr) {
+__device__ __forceinline__ void encode_all(const __half2* __restrict__ table, const uint4* __restrict__ rec,
+                                           uint32_t T, uint32_t dense_mask, const float3& x, bool has,
+                                           uint32_t taddr) {
+  static_assert(kRecLevels == 7, "encode_all reads levels 0..6 from the records");
   uint32_t f[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) f[k] = 0u;
   if (has) {
-    f[0] = encode_level<0>(table, T, dense_mask, x);
-    f[1] = encode_level<1>(table, T, dense_mask, x);
-    f[2] = encode_level<2>(table, T, dense_mask, x);
-    f[3] = encode_level<3>(table, T, dense_mask, x);
-    f[4] = encode_level<4>(table, T, dense_mask, x);
-    f[5] = encode_level<5>(table, T, dense_mask, x);
-    f[6] = encode_level<6>(table, T, dense_mask, x);
+    f[0] = encode_level_rec<0>(rec, x);
+    f[1] = encode_level_rec<1>(rec, x);
+    f[2] = encode_level_rec<2>(rec, x);
+    f[3] = encode_level_rec<3>(rec, x);
+    f[4] = encode_level_rec<4>(rec, x);
+    f[5] = encode_level_rec<5>(rec, x);
+    f[6] = encode_level_rec<6>(rec, x);
     f[7] = encode_level<7>(table, T, dense_mask, x);
     f[8] = encode_level<8>(table, T, dense_mask, x);
     f[9] = encode_level<9>(table, T, dense_mask, x);
@@ -179,17 +220,18 @@ __device__ __forceinline__ void mma_layer(uint32_t d_tmem, uint32_t a_tmem, uint
     tc::mma_f16_at(d_tmem, a_tmem + j * 8, tc::sdesc(b + j * 256, 128, K * 16), idesc, j > 0 ? 1u : 0u);
 }
 
-// 64 accumulator columns -> ReLU -> FP16 -> 32 hidden-activation columns, in
-// four 16-column slices so that few registers are live at once.
+// 64 accumulator columns -> ReLU -> FP16 -> 32 hidden-activation columns in
+// two 32-column rounds; the stores are not waited for here (the caller's
+// sync waits once for all of them).
 __device__ __forceinline__ void relu_to_h(uint32_t d_row, uint32_t h_row) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    float v[16];
-    tc::tmem_ld16(d_row + 16 * q, v);
-    uint32_t w[8];
+  for (int half = 0; half < 2; ++half) {
+    float v[32];
+    tc::tmem_ld32(d_row + 32 * half, v);
+    uint32_t w[16];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) w[k] = pk_relu(v[2 * k], v[2 * k + 1]);
-    tc::tmem_st8(h_row + 8 * q, w);
+    for (int k = 0; k < 16; ++k) w[k] = pk_relu(v[2 * k], v[2 * k + 1]);
+    tc::tmem_st16_nowait(h_row + 16 * half, w);
   }
 }
 
@@ -297,28 +339,35 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
 
     // Issues one layer (one thread) and waits for it (every thread); the
     // free barrier of the tile's buffer, if given, is released by the same
-    // completion.
-    auto layer = [&](uint32_t a_tmem, uint32_t b_off, int K, uint32_t idesc, uint64_t* also) -> bool {
+    // completion.  A failed wait is reported at the next sync().
+    bool ok = true;
+    auto layer = [&](uint32_t a_tmem, uint32_t b_off, int K, uint32_t idesc, uint64_t* also) {
       if (row == 0) {
         tc::fence_after();
         mma_layer(d_col, a_tmem, sW + b_off, K, idesc);
         tc::mma_commit(bar + 4);
         if (also) tc::mma_commit(also);
       }
-      const bool ok = tc::mbar_wait(bar + 4, pm);
+      ok = tc::mbar_wait(bar + 4, pm) && ok;
       pm ^= 1u;
       tc::fence_after();
-      return ok;
     };
-    // This thread's TMEM writes -> visible to the next MMA.
-    auto publish = [&]() {
+    // This thread's TMEM writes -> visible to the next MMA; true when any
+    // MLP thread of the group saw a wait fail (all of them then stop
+    // together, so no thread is left at a named barrier).
+    auto sync_bad = [&]() -> bool {
+      tc::tmem_wait_st();
       tc::fence_before();
-      tc::named_sync(mlp_bar, kRoleThreads);
+      return tc::named_sync_or(mlp_bar, kRoleThreads, !ok);
     };
 
     for (uint32_t k = 0;; ++k) {
       const int b = (int)(k & 1u);
-      if (!tc::mbar_wait_sleep(bar + b, (k >> 1) & 1u)) { fail = true; break; }
+      // Only row 0 waits for the tile; the barrier hands its outcome to the
+      // others.  (Were every thread to poll, one that fell two phases behind
+      // would wait for a phase that had already come round.)
+      if (row == 0) ok = tc::mbar_wait_sleep(bar + b, (k >> 1) & 1u);
+      if (sync_bad()) { fail = true; break; }
       tc::fence_after();
       if (wfin[b * 4 + 0] & wfin[b * 4 + 1] & wfin[b * 4 + 2] & wfin[b * 4 + 3]) {
         // Every encoder warp of the group is out of rays: release the
@@ -333,10 +382,10 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
       const float4 di = info[b * 128 + row];
       const uint32_t a_col = enc_cols + 16 * b;  // encoded features of this tile
       // density 32 -> 64 -> 16 (the first layer is the features' last reader)
-      if (!layer(a_col, kWoffDW1, 32, id64, bar + 2 + b)) { fail = true; break; }
+      layer(a_col, kWoffDW1, 32, id64, bar + 2 + b);
       relu_to_h(d_row, h_row);
-      publish();
-      if (!layer(h_col, kWoffDW2, 64, id16, nullptr)) { fail = true; break; }
+      if (sync_bad()) { fail = true; break; }
+      layer(h_col, kWoffDW2, 64, id16, nullptr);
       float sigma;
       {
         // colour input [SH16(d) | density outputs 1..15 | 0] -> h (layer 2
@@ -348,22 +397,22 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
 #pragma unroll
         for (int j = 0; j < 7; ++j) w[j] = pk(v[1 + 2 * j], v[2 + 2 * j]);
         w[7] = pk(v[15], 0.0f);
-        tc::tmem_st8(h_row + 8, w);
+        tc::tmem_st8_nowait(h_row + 8, w);
         float sh[16];
         sh16(make_float3(di.x, di.y, di.z), sh);
 #pragma unroll
         for (int j = 0; j < 8; ++j) w[j] = pk(sh[2 * j], sh[2 * j + 1]);
-        tc::tmem_st8(h_row, w);
+        tc::tmem_st8_nowait(h_row, w);
       }
-      publish();
+      if (sync_bad()) { fail = true; break; }
       // colour 32 -> 64 -> 64 -> 3
-      if (!layer(h_col, kWoffCW1, 32, id64, nullptr)) { fail = true; break; }
+      layer(h_col, kWoffCW1, 32, id64, nullptr);
       relu_to_h(d_row, h_row);
-      publish();
-      if (!layer(h_col, kWoffCW2, 64, id64, nullptr)) { fail = true; break; }
+      if (sync_bad()) { fail = true; break; }
+      layer(h_col, kWoffCW2, 64, id64, nullptr);
       relu_to_h(d_row, h_row);
-      publish();
-      if (!layer(h_col, kWoffCW3, 64, id16, nullptr)) { fail = true; break; }
+      if (sync_bad()) { fail = true; break; }
+      layer(h_col, kWoffCW3, 64, id16, nullptr);
       float v5[16];
       tc::tmem_ld16(d_row, v5);
       // Compositing (FP32, every operation rounded explicitly).
@@ -391,8 +440,7 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
         }
       }
       // The next tile's first layer overwrites the accumulator this thread
-      // has just read.
-      publish();
+      // has just read: the wait at the top of the loop is a barrier.
     }
   } else if (!fail) {
     // ======================= encoder warps =======================
@@ -406,11 +454,13 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
     for (uint32_t k = 0;; ++k) {
       const int b = (int)(k & 1u);
       if (k >= 2) {
-        bool ok = true;
-        if (lane == 0) ok = tc::mbar_wait_sleep(bar + 2 + b, ((k >> 1) - 1u) & 1u);
-        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-        if (!ok) { fail = true; break; }
-        if (*gdone) break;
+        // Lane 0 waits and reads the group's stop flag; the warp learns both
+        // from it, so every lane takes the same exit.
+        int st = 0;
+        if (lane == 0) st = !tc::mbar_wait_sleep(bar + 2 + b, ((k >> 1) - 1u) & 1u) ? 1 : (*gdone ? 2 : 0);
+        st = __shfl_sync(0xffffffffu, st, 0);
+        if (st == 1) { fail = true; break; }
+        if (st == 2) break;
       }
       // A ray the MLP terminated early (T < 1e-4) is encoded no further.
       if (q.live && term[row] == q.id + 1u) q.live = false;
@@ -450,7 +500,7 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
       uint32_t tag = 0;
       const float t = has ? fmaf((float)q.ei + 0.5f, kDt, q.ts) : 0.0f;
       const float3 x = sample_pos(q.o, q.d, t);
-      encode_all(sc.table16, sc.T, sc.dense_mask, x, has, enc_cols + 16 * b + lane_off);
+      encode_all(sc.table16, sc.rec16, sc.T, sc.dense_mask, x, has, enc_cols + 16 * b + lane_off);
       if (has) {
         tag = kTagSample | (q.first ? kTagFirst : 0u);
         q.first = false;
@@ -505,7 +555,43 @@ __global__ void pack_tc_weights_kernel(const float* __restrict__ w, uint8_t* __r
   *reinterpret_cast<__half*>(out + base + op_chunk(n, k >> 3, K) + (k & 7) * 2) = __float2half_rn(v);
 }
 
+// One thread per cell of the record levels: copies the cell's 8 corner
+// entries (same index rule as encode_level) into its 32-byte record.
+__global__ void build_records_kernel(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
+                                     uint4* __restrict__ rec) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < kRecCells; c += gridDim.x * blockDim.x) {
+    int L = 0;
+    while (L + 1 < kRecLevels && c >= rec_cell_offset(L + 1)) ++L;
+    const uint32_t N = (uint32_t)level_res(L), local = c - rec_cell_offset(L);
+    const uint32_t ix = local % N, iy = (local / N) % N, iz = local / (N * N);
+    uint32_t e[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t x = ix + (k & 1), y = iy + ((k >> 1) & 1), z = iz + ((k >> 2) & 1);
+      uint32_t idx;
+      if ((dense_mask >> L) & 1u) {
+        const uint32_t s = N + 1u;
+        idx = x + s * (y + s * z);
+      } else {
+        idx = (x ^ (y * kPrime1) ^ (z * kPrime2)) & (T - 1u);
+      }
+      const __half2 v = table[(size_t)L * T + idx];
+      e[k] = *reinterpret_cast<const uint32_t*>(&v);
+    }
+    rec[2 * (size_t)c] = make_uint4(e[0], e[1], e[2], e[3]);
+    rec[2 * (size_t)c + 1] = make_uint4(e[4], e[5], e[6], e[7]);
+  }
+}
+
 }  // namespace
+
+size_t tc_record_bytes() { return (size_t)kRecCells * 32; }
+
+cudaError_t launch_build_records(const __half2* table16, uint32_t T, uint32_t dense_mask, uint4* rec,
+                                 cudaStream_t stream) {
+  build_records_kernel<<<2048, 256, 0, stream>>>(table16, T, dense_mask, rec);
+  return cudaGetLastError();
+}
 
 size_t tc_weight_bytes() { return kWBytes; }
 
@@ -516,7 +602,7 @@ cudaError_t launch_pack_tc_weights(const float* w32, uint8_t* out, cudaStream_t 
 
 cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
                             cudaStream_t stream) {
-  if (!scene.table16 || !scene.tc_weights) return cudaErrorInvalidValue;
+  if (!scene.table16 || !scene.rec16 || !scene.tc_weights) return cudaErrorInvalidValue;
   static bool attr_set = false;  // idempotent; a race only repeats the calls
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRequest);

@@ -93,6 +93,7 @@ int on_ctx_stream(nes_ctx* c, void* user, Fn fn) {
 void free_ctx(nes_ctx* c) {
   cudaFree(c->d_table32);
   cudaFree(c->d_table16);
+  cudaFree(c->d_rec16);
   cudaFree(c->d_weights);
   cudaFree(c->d_tc_weights);
   cudaFree(c->d_occ);
@@ -199,9 +200,13 @@ int nes_create(const nes_config* cfg, nes_ctx** out) {
   if (cfg->precision == NES_PREC_FP16_TC) {
     if ((rc = dalloc(&c->d_table16, entries)) != NES_OK) return fail(rc);
     if (launch_table_to_fp16(c->d_table32, c->d_table16, entries, c->stream) != cudaSuccess) return fail(NES_EIO);
+    if ((rc = dalloc(&c->d_rec16, tc_record_bytes() / sizeof(uint4))) != NES_OK) return fail(rc);
+    if (launch_build_records(c->d_table16, host.T, c->scene.dense_mask, c->d_rec16, c->stream) != cudaSuccess)
+      return fail(NES_EIO);
     if ((rc = dalloc(&c->d_tc_weights, tc_weight_bytes())) != NES_OK) return fail(rc);
     if (launch_pack_tc_weights(c->d_weights, c->d_tc_weights, c->stream) != cudaSuccess) return fail(NES_EIO);
     c->scene.table16 = c->d_table16;
+    c->scene.rec16 = c->d_rec16;
     c->scene.tc_weights = c->d_tc_weights;
   }
   if (launch_occupancy(c->scene, kOccThreshold, c->d_occ, c->stream) != cudaSuccess) return fail(NES_EIO);

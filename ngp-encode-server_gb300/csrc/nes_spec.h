@@ -34,6 +34,18 @@ NES_HD constexpr int level_res(int l) {
        : l == 11 ? 561 : l == 12 ? 776 : l == 13 ? 1072 : l == 14 ? 1482 : 2048;
 }
 
+// Levels 0..kRecLevels-1 are also stored as per-cell records of their 8
+// corner entries for the tensor-core march: cells of level l start at
+// rec_cell_offset(l) (N_0^3 + ... + N_{l-1}^3); 2,190,575 cells, 70 MB.
+constexpr int kRecLevels = 7;
+NES_HD constexpr uint32_t rec_cell_offset(int l) {
+  uint32_t o = 0;
+  for (int j = 0; j < l; ++j) o += (uint32_t)level_res(j) * (uint32_t)level_res(j) * (uint32_t)level_res(j);
+  return o;
+}
+constexpr uint32_t kRecCells = rec_cell_offset(kRecLevels);
+static_assert(kRecCells == 2190575u, "record cells of levels 0..6");
+
 // Spatial-hash primes (Instant-NGP paper, Sec. 3).
 constexpr uint32_t kPrime1 = 2654435761u;
 constexpr uint32_t kPrime2 = 805459861u;
