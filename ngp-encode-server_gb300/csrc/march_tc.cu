@@ -5,19 +5,18 @@
 // specialisation.
 //
 // Why this shape: the march is bound by the ~128 scattered 4-byte table
-// gathers per sample, and their speed depends on the L1 cache; with more than
-// ~64 KiB of shared memory per SM the L1 shrinks below the coarse levels'
-// working set and the gathers run ~2.5x slower.  So shared memory holds only
-// the MLP weights (the B operands, 20 KiB) and small per-row hand-off arrays;
-// every A operand (encoded features, hidden layers, colour input) lives in
-// TMEM and feeds tcgen05.mma directly.
+// gathers per sample, and their speed depends on the L1 cache (a 28 KiB L1
+// made them ~2.5x slower than a 192 KiB one).  So shared memory holds only
+// the MLP weights (the B operands, 20 KiB) and small per-row hand-off arrays,
+// within the 32 KiB configuration; every A operand (encoded features, hidden
+// layers, colour input) lives in TMEM and feeds tcgen05.mma directly.
 //
 // One CTA per SM: 4 groups x (4 ENCODER warps + 4 MLP warps) = 1024 threads.
 //  - ENCODER thread = one ray slot.  Per tile it claims rays (a warp-wide
 //    chunk of 32 at a time), encodes its slot's next occupied sample from the
 //    FP16 table, writes the 32 FP16 features as its TMEM lane of the tile (16
-//    columns), hands the row's ray id, flags, direction and t over in shared
-//    memory and marks the tile full.  It never waits for results: only for
+//    columns), hands the row's ray id, flags and t over in shared memory and
+//    marks the tile full.  It never waits for results: only for
 //    its tile buffer to be free again (two buffers), which the MLP's first
 //    layer releases through its MMA commit.  Encoder warps run independently.
 //  - MLP thread = TMEM lane = tile row.  One thread issues each layer
@@ -64,12 +63,13 @@ constexpr int kWoffCW2 = 10240;  // N=64, K=64
 constexpr int kWoffCW3 = 18432;  // N=16 (rows 3..15 zero), K=64
 constexpr int kWBytes = 20480;
 
-// Per-group shared memory: per-row hand-off (direction + t, ray id + flags)
-// for both tile buffers, per-warp "out of rays" flags, early-termination
-// notices, the group's stop flag and mbarriers.
-constexpr int kGOffInfo = 0;                          // [2][128] float4 (d, t)
-constexpr int kGOffTag = kGOffInfo + 2 * 128 * 16;    // [2][128] uint2 (ray id, flags)
-constexpr int kGOffFin = kGOffTag + 2 * 128 * 8;      // [2][4] uint32
+// Per-group shared memory: the per-row hand-off of both tile buffers (ray id
+// with the flags in its top bits, and t), per-warp "out of rays" flags,
+// early-termination notices, the group's stop flag and mbarriers.  The whole
+// CTA stays within the 32 KiB shared-memory configuration, which leaves the
+// rest of the SM's 256 KiB as L1 for the hash-table gathers.
+constexpr int kGOffHand = 0;                          // [2][128] uint2 (id | flags << 28, t)
+constexpr int kGOffFin = kGOffHand + 2 * 128 * 8;     // [2][4] uint32
 constexpr int kGOffTerm = kGOffFin + 32;              // [128] uint32
 constexpr int kGOffDone = kGOffTerm + 128 * 4;        // uint32
 constexpr int kGOffBar = (kGOffDone + 4 + 7) / 8 * 8; // full0, full1, free0, free1, mma
@@ -80,9 +80,11 @@ constexpr int kOffGroups = kOffW + kWBytes;
 constexpr int kOffBarW = kOffGroups + kGroups * kGroupBytes;
 constexpr int kOffSlot = kOffBarW + 8;
 constexpr int kSmemUsed = kOffSlot + 8;
-constexpr int kSmemRequest = kSmemUsed + 1024;  // slack to align the base to 1 KiB
-// Keep the shared-memory carve-out at the 64 KiB configuration (L1 >= 192 KiB).
-static_assert(kSmemRequest + 1024 <= 64 * 1024, "shared memory above the L1-friendly carve-out");
+constexpr int kSmemAlign = 128;  // operand images need 16 B, mbarriers 8 B
+constexpr int kSmemRequest = kSmemUsed + kSmemAlign;
+// 1 KiB of each CTA's shared memory is reserved by the system.
+static_assert(kSmemRequest + 1024 <= 32 * 1024, "shared memory above the 32 KiB configuration");
+constexpr uint32_t kIdMask = (1u << 28) - 1u;  // ray ids < 2^27 (max_pixels bound)
 
 // Byte offset of 16-byte chunk c (K elements 8c..8c+7) of row n in a
 // K-major shared-memory operand with K columns (core matrices 8 rows x 16 B,
@@ -266,16 +268,16 @@ __device__ __forceinline__ void skip_empty(const DevScene& sc, Slot& q) {
 
 __global__ void __launch_bounds__(kTcThreads, 1)
 march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
-  extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + kSmemAlign - 1) &
+                                             ~uintptr_t(kSmemAlign - 1));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = tid / kGroupThreads;
   const bool is_mlp = (tid % kGroupThreads) >= kRoleThreads;
   const int row = tid % kRoleThreads;  // tile row = TMEM lane
   uint8_t* G = smem + kOffGroups + g * kGroupBytes;
   uint64_t* bar = reinterpret_cast<uint64_t*>(G + kGOffBar);  // full0, full1, free0, free1, mma
-  float4* info = reinterpret_cast<float4*>(G + kGOffInfo);    // [2][128] (d, t)
-  uint2* tagw = reinterpret_cast<uint2*>(G + kGOffTag);       // [2][128] (ray id, flags)
+  uint2* hand = reinterpret_cast<uint2*>(G + kGOffHand);      // [2][128] (id | flags << 28, t)
   uint32_t* wfin = reinterpret_cast<uint32_t*>(G + kGOffFin); // [2][4] encoder warp finished
   uint32_t* term = reinterpret_cast<uint32_t*>(G + kGOffTerm);  // [128] early-terminated ray id + 1
   volatile uint32_t* gdone = reinterpret_cast<volatile uint32_t*>(G + kGOffDone);
@@ -336,6 +338,7 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
     uint32_t pm = 0;
     uint32_t cur = 0xFFFFFFFFu;  // ray being composited in this row (none)
     float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f, cz = 0.0f;
+    float dx = 0.0f, dy = 0.0f, dz = 1.0f;  // direction of the row's current ray
 
     // Issues one layer (one thread) and waits for it (every thread); the
     // free barrier of the tile's buffer, if given, is released by the same
@@ -378,8 +381,15 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
         }
         break;
       }
-      const uint2 tg = tagw[b * 128 + row];
-      const float4 di = info[b * 128 + row];
+      const uint2 hd = hand[b * 128 + row];
+      const uint32_t rid = hd.x & kIdMask, flags = hd.x >> 28;
+      const float t = __uint_as_float(hd.y);
+      if (flags & kTagFirst) {  // a new ray in this row: its direction, for the colour MLP
+        const float4 rd = s.ray_dt[rid];
+        dx = rd.x;
+        dy = rd.y;
+        dz = rd.z;
+      }
       const uint32_t a_col = enc_cols + 16 * b;  // encoded features of this tile
       // density 32 -> 64 -> 16 (the first layer is the features' last reader)
       layer(a_col, kWoffDW1, 32, id64, bar + 2 + b);
@@ -399,7 +409,7 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
         w[7] = pk(v[15], 0.0f);
         tc::tmem_st8_nowait(h_row + 8, w);
         float sh[16];
-        sh16(make_float3(di.x, di.y, di.z), sh);
+        sh16(make_float3(dx, dy, dz), sh);
 #pragma unroll
         for (int j = 0; j < 8; ++j) w[j] = pk(sh[2 * j], sh[2 * j + 1]);
         tc::tmem_st8_nowait(h_row, w);
@@ -416,25 +426,25 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
       float v5[16];
       tc::tmem_ld16(d_row, v5);
       // Compositing (FP32, every operation rounded explicitly).
-      if (tg.y & kTagSample) {
-        if (tg.y & kTagFirst) {
-          cur = tg.x;
+      if (flags & kTagSample) {
+        if (flags & kTagFirst) {
+          cur = rid;
           T = 1.0f;
           cr = cg = cb = cz = 0.0f;
         }
-        if (cur == tg.x) {  // samples of a ray that already terminated are dropped
+        if (cur == rid) {  // samples of a ray that already terminated are dropped
           ++my_samples;
           const float alpha = -expm1f(__fmul_rn(-sigma, kDt));
           const float wgt = __fmul_rn(T, alpha);
           cr = __fmaf_rn(wgt, sigmoidf(v5[0]), cr);
           cg = __fmaf_rn(wgt, sigmoidf(v5[1]), cg);
           cb = __fmaf_rn(wgt, sigmoidf(v5[2]), cb);
-          cz = __fmaf_rn(wgt, di.w, cz);
+          cz = __fmaf_rn(wgt, t, cz);
           T = __fsub_rn(T, wgt);
           const bool stop_early = T < kTStop;
-          if (stop_early || (tg.y & kTagLast)) {
+          if (stop_early || (flags & kTagLast)) {
             write_ray(vb, s, cur, cr, cg, cb, cz);
-            if (stop_early && !(tg.y & kTagLast)) term[row] = cur + 1u;  // tells the encoder to move on
+            if (stop_early && !(flags & kTagLast)) term[row] = cur + 1u;  // tells the encoder to move on
             cur = 0xFFFFFFFFu;
           }
         }
@@ -511,8 +521,7 @@ march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
           q.live = false;
         }
       }
-      info[b * 128 + row] = make_float4(q.d.x, q.d.y, q.d.z, t);
-      tagw[b * 128 + row] = make_uint2(q.id, tag);
+      hand[b * 128 + row] = make_uint2(q.id | (tag << 28), __float_as_uint(t));
       const bool fin = exhausted && __ballot_sync(0xffffffffu, has) == 0u;
       if (lane == 0) wfin[b * 4 + wq] = fin ? 1u : 0u;
       tc::tmem_wait_st();
@@ -603,13 +612,14 @@ cudaError_t launch_pack_tc_weights(const float* w32, uint8_t* out, cudaStream_t 
 cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
                             cudaStream_t stream) {
   if (!scene.table16 || !scene.rec16 || !scene.tc_weights) return cudaErrorInvalidValue;
+  if (s.max_rays > kIdMask) return cudaErrorInvalidValue;  // ray ids share a word with the flags
   static bool attr_set = false;  // idempotent; a race only repeats the calls
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRequest);
     if (e != cudaSuccess) return e;
-    // Smallest carve-out that holds the request: the rest of the SM's
-    // 256 KiB stays L1 for the hash-table gathers.
-    e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+    // 14 % of 228 KiB selects the 32 KiB configuration, which holds the
+    // request: the rest of the SM's 256 KiB stays L1 for the table gathers.
+    e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 14);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
