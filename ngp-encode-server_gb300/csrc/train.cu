@@ -22,7 +22,10 @@
 //  3. backward (thread per record, in chunks): recompute the encoding and
 //     both MLPs, backpropagate, scatter-add the encoding gradient into the
 //     FP32 gradient table with float2 atomics, and stage every layer's input
-//     activations and output deltas;
+//     activations and output deltas.  By default the ten layer products of
+//     the recompute and the backpropagation run on the tensor cores
+//     (backward_tc_kernel, tcgen05 kind::tf32); exact_weight_grads = 1 keeps
+//     them in FP32 on the CUDA cores (backward_kernel);
 //  4. weight gradients: per layer dW[out][in] += sum_s delta[s][out] act[s][in]
 //     over the chunk (dw_kernel, register-tiled split-K reduction);
 //  5. Adam on the table and the weights (bias-corrected); gradients zeroed.
@@ -705,6 +708,341 @@ dw_tc_kernel(Staging st, uint32_t ntiles, float* __restrict__ dw, uint32_t* __re
   if (warp == 1) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
+// ---------------- per-sample MLP recompute and backward on the tensor cores (kind::tf32) ----------------
+// One CTA per SM, four independent groups of 4 warps; a group takes 128
+// records at a time (thread = record = TMEM lane) and runs the 10 layer
+// products of the recompute and the backward as tcgen05.mma kind::tf32 with
+// the A operand (this layer's input, one FP32 element per TMEM column) in
+// TMEM and B (a weight image, below) in shared memory, the FP32 product in
+// TMEM.  Between products each thread reads its row back, applies the
+// elementwise step (ReLU and its mask, exp, SH, sigmoid and their
+// derivatives), stages activations and deltas for the weight-gradient GEMMs
+// (same layout as backward_kernel) and writes the next A.  TF32 operands
+// (10-bit mantissa, FP32 accumulation) put ~1e-3 relative error on the
+// per-sample activations and deltas; backward_kernel is the FP32 form.
+//   forward:  h1 = relu(enc dW1^T)  out = h1 dW2^T  g1 = relu(cin cW1^T)
+//             g2 = relu(g1 cW2^T)   logit = g2 cW3^T
+//   backward: dg2 = (dlog cW3) m2   dg1 = (dg2 cW2) m1   dgeo = dg1 cW1[:,16:32]
+//             dh1 = (dout dW2) mh   denc = dh1 dW1
+constexpr int kBtGroups = 4;
+constexpr int kBtThreads = 128 * kBtGroups;
+constexpr uint32_t kBtColsPerGroup = 128;  // A: 64 columns, D: 64 columns
+constexpr int kAggLevels = 7;  // levels whose scatter-add is warp-aggregated (N <= 111)
+static_assert(level_res(kAggLevels - 1) < 128, "cell key packs 7 bits per coordinate");
+
+// Weight images, [N][K] K-major, no swizzle, FP32 bits read as TF32: core
+// matrices of 8 rows x 4 elements (16 B rows, 128 B each), K-adjacent at
+// 128 B (LBO), 8-row groups K/4 x 128 B apart (SBO).
+__host__ __device__ constexpr uint32_t tf32_off(int n, int k, int K) {
+  return (uint32_t)((n >> 3) * (K * 32) + (k >> 2) * 128 + (n & 7) * 16 + (k & 3) * 4);
+}
+struct BtImage {
+  uint32_t off, N, K;
+};
+constexpr int kBtImages = 10;
+// dW1, dW2, cW1, cW2, cW3 (rows 3..15 zero), cW3^T (k 3..15 zero), cW2^T,
+// cW1 geometry columns transposed ([n][j] = cW1[j][16 + n], row 15 zero),
+// dW2^T, dW1^T.
+__host__ __device__ constexpr BtImage bt_image(int i) {
+  return i == 0   ? BtImage{0, 64, 32}
+         : i == 1 ? BtImage{8192, 16, 64}
+         : i == 2 ? BtImage{12288, 64, 32}
+         : i == 3 ? BtImage{20480, 64, 64}
+         : i == 4 ? BtImage{36864, 16, 64}
+         : i == 5 ? BtImage{40960, 64, 16}
+         : i == 6 ? BtImage{45056, 64, 64}
+         : i == 7 ? BtImage{61440, 16, 64}
+         : i == 8 ? BtImage{65536, 64, 16}
+                  : BtImage{69632, 32, 64};
+}
+constexpr uint32_t kBtImageBytes = 77824;
+static_assert(bt_image(9).off + bt_image(9).N * bt_image(9).K * 4 == kBtImageBytes, "image table");
+
+// Value of element (n, k) of image i from the FP32 weight blob.
+__device__ __forceinline__ float bt_value(const float* __restrict__ w, int i, int n, int k) {
+  switch (i) {
+    case 0: return w[kOffDW1 + n * kEnc + k];
+    case 1: return w[kOffDW2 + n * kHid + k];
+    case 2: return w[kOffCW1 + n * kCIn + k];
+    case 3: return w[kOffCW2 + n * kHid + k];
+    case 4: return n < 3 ? w[kOffCW3 + n * kHid + k] : 0.0f;
+    case 5: return k < 3 ? w[kOffCW3 + k * kHid + n] : 0.0f;
+    case 6: return w[kOffCW2 + k * kHid + n];
+    case 7: return n < 15 ? w[kOffCW1 + k * kCIn + 16 + n] : 0.0f;
+    case 8: return w[kOffDW2 + k * kHid + n];
+    default: return w[kOffDW1 + k * kEnc + n];
+  }
+}
+
+__global__ void pack_bt_images_kernel(const float* __restrict__ w, uint8_t* __restrict__ img) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;  // element of the concatenated images
+  if (e >= kBtImageBytes / 4) return;
+  int i = 0;
+  while (i + 1 < kBtImages && e >= bt_image(i + 1).off / 4) ++i;
+  const BtImage b = bt_image(i);
+  const uint32_t local = e - b.off / 4;
+  const int n = (int)(local / b.K), k = (int)(local % b.K);
+  *reinterpret_cast<float*>(img + b.off + tf32_off(n, k, (int)b.K)) = bt_value(w, i, n, k);
+}
+
+__device__ __forceinline__ uint32_t f2u(float v) { return __float_as_uint(v); }
+
+__global__ void __launch_bounds__(kBtThreads, 1)
+backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t count,
+                   const TrainRay* __restrict__ rays, const DevScene sc, const uint8_t* __restrict__ images,
+                   Staging st, float2* __restrict__ gtable, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(128) uint8_t smem_bt[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_bt + kBtImageBytes);  // [group] mma, [kBtGroups] weights
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kBtGroups + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, row = tid & 127;
+  if (tid == 0) {
+    for (int k = 0; k <= kBtGroups; ++k) tc::mbar_init(bars + k, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, kBtColsPerGroup * kBtGroups);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tslot;
+  bool fail = false;
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(bars + kBtGroups, kBtImageBytes);
+    tc::bulk_g2s(smem_bt, images, kBtImageBytes, bars + kBtGroups);
+    fail = !tc::mbar_wait(bars + kBtGroups, 0);
+  }
+  fail = __syncthreads_or(fail);
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+  const uint32_t a_col = tmem + g * kBtColsPerGroup, d_col = a_col + 64;
+  const uint32_t a_row = a_col + lane_off, d_row = d_col + lane_off;
+  const uint32_t sB = tc::smem_addr(smem_bt);
+  const uint32_t gbar = 1 + g;
+  uint64_t* mbar = bars + g;
+  uint32_t pm = 0;
+  bool ok = true;
+  // D[:, :N] = A[:, :K] B_i^T.  Every thread publishes its TMEM writes; the
+  // group learns of any failed wait here and stops as a whole.
+  auto mma = [&](int i) -> bool {
+    tc::tmem_wait_st();
+    tc::fence_before();
+    if (tc::named_sync_or(gbar, 128, !ok)) return false;
+    const BtImage b = bt_image(i);
+    if (row == 0) {
+      tc::fence_after();
+      const uint32_t idesc = tc::idesc_tf32_f32(128, (int)b.N);
+      for (uint32_t j = 0; j < b.K / 8; ++j)
+        tc::mma_tf32_at(d_col, a_col + 8 * j, tc::sdesc(sB + b.off + 256 * j, 128, b.K * 32), idesc, j > 0 ? 1u : 0u);
+      tc::mma_commit(mbar);
+    }
+    ok = tc::mbar_wait(mbar, pm) && ok;
+    pm ^= 1u;
+    tc::fence_after();
+    return true;
+  };
+
+  const uint32_t ntiles = (count + 127u) / 128u;
+  const uint32_t staged = (count + 31u) & ~31u;  // rows the weight-gradient GEMMs read
+  if (!fail) {
+    for (uint32_t tile = blockIdx.x * kBtGroups + g; tile < ntiles; tile += gridDim.x * kBtGroups) {
+      const uint32_t s = tile * 128u + (uint32_t)row;
+      const bool valid = s < count, stage = s < staged;
+      SampleRec q;
+      if (valid) {
+        q = recs[first + s];
+      } else {
+        q.x = q.y = q.z = 0.0f;
+        q.ray = 0;
+        q.dsigma = q.dcr = q.dcg = q.dcb = 0.0f;
+      }
+      const float3 x = make_float3(q.x, q.y, q.z);
+      uint32_t u[32];
+      float v[32];
+      // ---- forward recompute ----
+      {
+        float enc[kEnc];
+        if (valid) {
+          encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
+        } else {
+#pragma unroll
+          for (int k = 0; k < kEnc; ++k) enc[k] = 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < kEnc; ++k) {
+          if (stage) stage_row(st.enc, kEnc, s)[soff(k)] = enc[k];
+          u[k] = f2u(enc[k]);
+        }
+        tc::tmem_st32_nowait(a_row, u);
+      }
+      if (!mma(0)) break;
+      uint64_t m_h1 = 0, m_g1 = 0, m_g2 = 0;
+      // ReLU of D[:, :64] -> staging, mask, next A.
+      auto relu64 = [&](float* r_act, uint64_t& m) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          tc::tmem_ld32(d_row + 32 * c, v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float a = valid ? fmaxf(v[j], 0.0f) : 0.0f;
+            m |= (uint64_t)(a > 0.0f) << (32 * c + j);
+            if (stage) r_act[soff(32 * c + j)] = a;
+            u[j] = f2u(a);
+          }
+          tc::tmem_st32_nowait(a_row + 32 * c, u);
+        }
+      };
+      relu64(stage_row(st.h1, kHid, s), m_h1);
+      if (!mma(1)) break;
+      float sigma;
+      {
+        float out[16];
+        tc::tmem_ld16(d_row, reinterpret_cast<float(&)[16]>(out));
+        sigma = expf(out[0] - 1.0f);
+        float cin[kCIn];
+        const TrainRay& r = rays[q.ray];
+        sh16(make_float3(r.dx, r.dy, r.dz), cin);
+#pragma unroll
+        for (int k = 0; k < 15; ++k) cin[16 + k] = out[1 + k];
+        cin[31] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kCIn; ++k) {
+          const float c = valid ? cin[k] : 0.0f;
+          if (stage) stage_row(st.cin, kCIn, s)[soff(k)] = c;
+          u[k] = f2u(c);
+        }
+        tc::tmem_st32_nowait(a_row, u);
+      }
+      if (!mma(2)) break;
+      relu64(stage_row(st.g1, kHid, s), m_g1);
+      if (!mma(3)) break;
+      relu64(stage_row(st.g2, kHid, s), m_g2);
+      if (!mma(4)) break;
+      // ---- backward ----
+      {
+        float lg[16];
+        tc::tmem_ld16(d_row, reinterpret_cast<float(&)[16]>(lg));
+        const float c0 = sigmoidf(lg[0]), c1 = sigmoidf(lg[1]), c2 = sigmoidf(lg[2]);
+        const float dl[3] = {q.dcr * c0 * (1.0f - c0), q.dcg * c1 * (1.0f - c1), q.dcb * c2 * (1.0f - c2)};
+        uint32_t w16[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) w16[k] = k < 3 ? f2u(dl[k]) : 0u;
+#pragma unroll
+        for (int k = 0; k < kFDlog; ++k)
+          if (stage) stage_row(st.dlog, kFDlog, s)[soff(k)] = k < 3 ? dl[k] : 0.0f;
+        tc::tmem_st16_nowait(a_row, w16);
+      }
+      // Masked D[:, :64] -> staging, next A.
+      auto mask64 = [&](float* r_d, uint64_t m) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          tc::tmem_ld32(d_row + 32 * c, v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float d = ((m >> (32 * c + j)) & 1u) ? v[j] : 0.0f;
+            if (stage) r_d[soff(32 * c + j)] = d;
+            u[j] = f2u(d);
+          }
+          tc::tmem_st32_nowait(a_row + 32 * c, u);
+        }
+      };
+      if (!mma(5)) break;
+      mask64(stage_row(st.dg2, kHid, s), m_g2);
+      if (!mma(6)) break;
+      mask64(stage_row(st.dg1, kHid, s), m_g1);
+      if (!mma(7)) break;
+      {
+        float geo[16];
+        tc::tmem_ld16(d_row, reinterpret_cast<float(&)[16]>(geo));
+        uint32_t w16[16];
+        const float d0 = q.dsigma * sigma;
+        w16[0] = f2u(d0);
+        if (stage) stage_row(st.dout, kDOut, s)[soff(0)] = d0;
+#pragma unroll
+        for (int m = 0; m < 15; ++m) {
+          w16[1 + m] = f2u(geo[m]);
+          if (stage) stage_row(st.dout, kDOut, s)[soff(1 + m)] = geo[m];
+        }
+        tc::tmem_st16_nowait(a_row, w16);
+      }
+      if (!mma(8)) break;
+      mask64(stage_row(st.dh1, kHid, s), m_h1);
+      if (!mma(9)) break;
+      tc::tmem_ld32(d_row, v);  // denc
+      // The next tile's first product overwrites D: its sync follows these reads.
+      // Hash-grid scatter-add.  A warp's 32 records are consecutive samples
+      // of one or two rays, so at the coarse levels runs of neighbouring
+      // lanes share a cell: levels 0..kAggLevels-1 sum each run's corner
+      // gradients with shuffles and add them with one atomic per run.
+      const uint32_t lane = (uint32_t)(tid & 31);
+#pragma unroll 1
+      for (int l = 0; l < kLevels; ++l) {
+        const int N = level_res(l);
+        const LevelCell c = level_cell(x, N);
+        uint32_t idx[8];
+        corner_indices(c, N, (sc.dense_mask >> l) & 1u, sc.T, idx);
+        float w[8];
+        corner_weights(c, w);
+        float2* gt = gtable + (size_t)l * sc.T;
+        float d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kLevels; ++k)
+          if (k == l) {
+            d0 = v[2 * k];
+            d1 = v[2 * k + 1];
+          }
+        if (l >= kAggLevels) {
+          if (valid)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
+          continue;
+        }
+        // Runs of lanes with the same cell (invalid lanes form runs of their
+        // own and add nothing).  N <= 111 here: 7 bits per coordinate.
+        const uint32_t key = valid ? (c.ix | (c.iy << 7) | (c.iz << 14)) : (0x80000000u | lane);
+        const uint32_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
+        const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != key);
+        if (heads == 0xffffffffu) {  // no lane shares its cell
+          if (valid)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
+          continue;
+        }
+        // Step o adds the partial sum of lane + o when no run starts in
+        // (lane, lane + o]; afterwards each run's first lane holds its total.
+        uint32_t take = 0;
+#pragma unroll
+        for (int o = 1, b = 0; o < 32; o <<= 1, ++b) {
+          const uint32_t span = (uint32_t)(((1ull << o) - 1ull) << (lane + 1));  // lanes lane+1 .. lane+o
+          if (lane + o < 32u && (heads & span) == 0u) take |= 1u << b;
+        }
+        const bool head = (heads >> lane) & 1u;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          float a0 = w[k] * d0, a1 = w[k] * d1;
+#pragma unroll
+          for (int o = 1, b = 0; o < 32; o <<= 1, ++b) {
+            const float p0 = __shfl_down_sync(0xffffffffu, a0, o), p1 = __shfl_down_sync(0xffffffffu, a1, o);
+            if ((take >> b) & 1u) {
+              a0 += p0;
+              a1 += p1;
+            }
+          }
+          if (valid && head) atomicAdd(gt + idx[k], make_float2(a0, a1));
+        }
+      }
+    }
+  }
+  if (fail || !ok) atomicExch(err, kErrTimeout);
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, kBtColsPerGroup * kBtGroups);
+  }
+}
+constexpr int kBtSmem = (int)kBtImageBytes + 8 * (kBtGroups + 1) + 16;
+
 __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
                             size_t n, float lr, float b1, float b2, float eps, float bc1, float bc2) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -840,6 +1178,7 @@ struct nes_trainer {
   float* d_gw = nullptr;
   float *d_mt = nullptr, *d_vt = nullptr, *d_mw = nullptr, *d_vw = nullptr;
   float* d_stage = nullptr;
+  uint8_t* d_bimg = nullptr;  // TF32 weight images of backward_tc_kernel
   uint32_t chunk = 0;
   int fwd_blocks = 0;  // persistent forward grid: SMs x resident blocks
   uint64_t steps = 0;
@@ -912,10 +1251,21 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   const Staging sg = staging(t);
   float* gw = t->d_gw;
   const int sms = c->num_sms;
+  if (!t->cfg.exact_weight_grads) {  // this step's weights as TF32 operand images
+    pack_bt_images_kernel<<<(kBtImageBytes / 4 + 255) / 256, 256, 0, t->st>>>(c->d_weights, t->d_bimg);
+    TR_CUDA(cudaGetLastError());
+  }
   for (uint32_t first = 0; first < total; first += t->chunk) {
     const uint32_t cnt = total - first < t->chunk ? total - first : t->chunk;
-    backward_kernel<<<(cnt + kBwdThreads - 1) / kBwdThreads, kBwdThreads, kSmemB, t->st>>>(t->d_recs, first, cnt, t->d_rays,
-                                                                                  c->scene, sg, t->d_gtable);
+    if (t->cfg.exact_weight_grads) {
+      backward_kernel<<<(cnt + kBwdThreads - 1) / kBwdThreads, kBwdThreads, kSmemB, t->st>>>(
+          t->d_recs, first, cnt, t->d_rays, c->scene, sg, t->d_gtable);
+    } else {
+      const uint32_t groups = (cnt + 127u) / 128u;
+      const uint32_t want = (groups + kBtGroups - 1) / kBtGroups;
+      backward_tc_kernel<<<want < (uint32_t)sms ? want : (uint32_t)sms, kBtThreads, kBtSmem, t->st>>>(
+          t->d_recs, first, cnt, t->d_rays, c->scene, t->d_bimg, sg, t->d_gtable, t->d_ctr + 1);
+    }
     TR_CUDA(cudaGetLastError());
     if (t->cfg.exact_weight_grads) {
       TR_CUDA((launch_dw<kEnc, kHid, kHid>(sg.enc, sg.dh1, cnt, gw + kOffDW1, sms, t->st)));
@@ -991,6 +1341,7 @@ void free_trainer(nes_trainer* t) {
   cudaFree(t->d_mw);
   cudaFree(t->d_vw);
   cudaFree(t->d_stage);
+  cudaFree(t->d_bimg);
   for (cudaEvent_t e : t->ev)
     if (e) cudaEventDestroy(e);
   if (t->st) cudaStreamDestroy(t->st);
@@ -1050,7 +1401,8 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaMalloc(&t->d_vt, nt * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&t->d_mw, kWeightFloats * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&t->d_vw, kWeightFloats * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&t->d_stage, (size_t)t->chunk * kStageFloats * sizeof(float)) != cudaSuccess)
+      cudaMalloc(&t->d_stage, (size_t)t->chunk * kStageFloats * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&t->d_bimg, kBtImageBytes) != cudaSuccess)
     return fail(NES_ENOMEM);
   if (cudaMemset(t->d_gtable, 0, nt * sizeof(float)) != cudaSuccess ||
       cudaMemset(t->d_gw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
@@ -1063,8 +1415,15 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
   if (cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess ||
       cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess ||
       cudaFuncSetAttribute(dw_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(DwTcSmem)) !=
-          cudaSuccess)
+          cudaSuccess ||
+      cudaFuncSetAttribute(backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBtSmem) != cudaSuccess)
     return fail(NES_EIO);
+  {
+    // backward_tc_kernel allocates all 512 TMEM columns: one CTA per SM,
+    // which its register footprint (512 threads x > 64) guarantees.
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, backward_tc_kernel) != cudaSuccess || fa.numRegs <= 64) return fail(NES_EIO);
+  }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_kernel, kFwdThreads, kSmemW) != cudaSuccess)
     return fail(NES_EIO);

@@ -6,11 +6,18 @@ loss curve and the error paths.
 Tolerances: loss relative 1e-5; gradients (FP32 accumulation with atomics
 in nondeterministic order against FP64) relative L2 error <= 1e-4 per
 parameter block and |delta| <= 1e-3 of the block's largest entry; finite
-differences relative 1e-3.  The default weight gradients are TF32 tensor-core
-GEMMs (10-bit mantissa operands, FP32 accumulation): their weight blocks are
-held to relative L2 5e-3 and 2e-2 of the largest entry, everything else to
-the FP32 tolerances; `exact_weight_grads=1` (FP32 CUDA cores) is held to the
-FP32 tolerances throughout."""
+differences relative 1e-3.  `exact_weight_grads=1` (per-sample MLP recompute,
+backpropagation and weight gradients in FP32 on the CUDA cores) is held to
+these FP32 tolerances throughout.  The default runs the ten per-sample layer
+products and the weight-gradient GEMMs on the tensor cores in TF32 (10-bit
+mantissa operands, FP32 accumulation).  Against the FP32 path on 4,096 rays
+it is held to relative L2 2e-2 and 5e-2 of the block's largest entry
+(TF32_REL, TF32_PEAK; measured 0.2-0.5 %).  Against the FP64 oracle on 64
+rays the fine levels' entries each gather one or two samples, and a hidden
+unit whose TF32 pre-activation lands on the other side of zero than in FP32
+changes that sample's whole contribution: measured 0.2-1.9 % relative L2 and
+up to 15 % of a block's largest entry, held to ORACLE_TF32 = (3e-2, 0.25).
+The loss, which the FP32 forward computes, keeps the FP32 tolerance."""
 import numpy as np
 import pytest
 
@@ -91,6 +98,10 @@ def _errs(a, b):
     return (np.linalg.norm(a - b) / nb if nb else np.linalg.norm(a), np.abs(a - b).max() / mb if mb else 0.0)
 
 
+TF32_REL, TF32_PEAK = 2e-2, 5e-2
+ORACLE_TF32 = (3e-2, 0.25)
+
+
 def _close(a, b, rel=1e-4, peak=1e-3):
     e_rel, e_peak = _errs(a, b)
     return e_rel <= rel and e_peak <= peak
@@ -100,19 +111,20 @@ def _close(a, b, rel=1e-4, peak=1e-3):
 def test_gradient_matches_oracle(nes_lib, oracle_mod, setup, exact):
     views, rgb, dep = setup
     r, t = _student(nes_lib, setup, exact_weight_grads=exact)
-    wrel, wpeak = (1e-4, 1e-3) if exact else (5e-3, 2e-2)
+    rel, peak = (1e-4, 1e-3) if exact else ORACLE_TF32
     pairs = _pairs(64, len(views), 3)
     loss, gt, gw = t.grad(pairs, TABLE_FLOATS)
     samples = t.last_samples()
     oloss, ogt, ogw, ocount = _oracle_grad(oracle_mod, r, views, pairs, rgb, dep)
     assert samples == ocount
     assert abs(loss - oloss) <= 1e-5 * oloss
-    bad = [(name, _errs(gw[a:b], ogw[a:b])) for name, (a, b) in BLOCKS.items()
-           if not _close(gw[a:b], ogw[a:b], wrel, wpeak)]
+    errs = {name: _errs(gw[a:b], ogw[a:b]) for name, (a, b) in BLOCKS.items()}
     for lvl in range(16):
         seg = slice(lvl * (1 << LOG2T) * 2, (lvl + 1) * (1 << LOG2T) * 2)
-        if not _close(gt[seg], ogt[seg]):
-            bad.append((lvl, _errs(gt[seg], ogt[seg])))
+        errs[lvl] = _errs(gt[seg], ogt[seg])
+    print("gradient errors vs FP64 oracle (exact=%d):" % exact,
+          {k: (round(float(a), 6), round(float(b), 6)) for k, (a, b) in errs.items()})
+    bad = [(k, e) for k, e in errs.items() if not (e[0] <= rel and e[1] <= peak)]
     assert not bad, bad
     # The gradient call changes nothing: a second call gives the same loss.
     loss2, _, _ = t.grad(pairs, TABLE_FLOATS)
@@ -151,8 +163,9 @@ def test_gradient_matches_gpu_finite_differences(nes_lib, setup):
 
 
 def test_tensor_core_weight_gradients_match_exact(nes_lib, setup):
-    """4,096 rays (~0.9 M samples, ~28 k tiles): every CTA of the TF32 kernel
-    wraps its 3-stage ring many times and ends on a partial tile."""
+    """4,096 rays (~0.9 M samples, ~28 k weight-gradient tiles, ~7 k
+    backward tiles): every CTA of the TF32 kernels wraps its loop many times
+    and ends on a partial tile."""
     views, rgb, dep = setup
     pairs = _pairs(4096, len(views), 7)
     out = {}
@@ -163,9 +176,11 @@ def test_tensor_core_weight_gradients_match_exact(nes_lib, setup):
         r.close()
     (l1, gt1, gw1), (l0, gt0, gw0) = out[1], out[0]
     assert l0 == pytest.approx(l1, rel=1e-6)
-    assert _close(gt0, gt1, 1e-5, 1e-4), _errs(gt0, gt1)
+    print("tensor-core vs FP32 gradients: table", _errs(gt0, gt1),
+          {name: _errs(gw0[a:b], gw1[a:b]) for name, (a, b) in BLOCKS.items()})
+    assert _close(gt0, gt1, TF32_REL, TF32_PEAK), _errs(gt0, gt1)
     bad = [(name, _errs(gw0[a:b], gw1[a:b])) for name, (a, b) in BLOCKS.items()
-           if not _close(gw0[a:b], gw1[a:b], 5e-3, 2e-2)]
+           if not _close(gw0[a:b], gw1[a:b], TF32_REL, TF32_PEAK)]
     assert not bad, bad
 
 
