@@ -308,6 +308,22 @@ int nes_gray8_to_yuv420p(const uint8_t *gray_dev, int width, int height, int gra
                          uint8_t *y_dev, uint8_t *u_dev, uint8_t *v_dev, const int linesize[3],
                          void *stream);
 
+/* Batched frame glue.  neserver converts one frame per call (process_frame_thread
+ * -> RenderedFrame::convert_frame, src/encode.cpp:42-119); these convert
+ * nframes frames of one geometry in a single launch, each frame identical to
+ * the single-frame call.  rgb_dev / gray_dev / y_dev / u_dev / v_dev (and
+ * depth_dev / out_dev) are host arrays of nframes device pointers; at most
+ * NES_MAX_BATCH_FRAMES frames per call. */
+#define NES_MAX_BATCH_FRAMES 64
+int nes_rgb24_to_yuv420p_batch(int nframes, const uint8_t *const *rgb_dev, int width, int height,
+                               int rgb_linesize, uint8_t *const *y_dev, uint8_t *const *u_dev,
+                               uint8_t *const *v_dev, const int linesize[3], void *stream);
+int nes_gray8_to_yuv420p_batch(int nframes, const uint8_t *const *gray_dev, int width, int height,
+                               int gray_linesize, uint8_t *const *y_dev, uint8_t *const *u_dev,
+                               uint8_t *const *v_dev, const int linesize[3], void *stream);
+int nes_depth_pack_u16mm_batch(int nframes, const float *const *depth_dev, size_t n, uint16_t *const *out_dev,
+                               void *stream);
+
 /* Debug text overlay into an RGB24 frame on the device, before conversion:
  * RenderTextContext::render_string_to_frame (src/base/video/render_text.cc:35-111)
  * with the same five anchors (margin 50, box 300x100), '\n' = back to the

@@ -104,9 +104,9 @@ __device__ __forceinline__ void rgb_block_scalar(const uint8_t* __restrict__ rgb
   V[(size_t)cy * ls2 + cx] = clamp8((kVR * sr + kVG * sg + kVB * sb + (128 << 18) + (1 << 17)) >> 18);
 }
 
-__global__ void __launch_bounds__(kGlueThreads)
-rgb24_to_yuv420p_v8_kernel(const uint8_t* __restrict__ rgb, int w, int h, int rgb_ls, uint8_t* __restrict__ Y,
-                           uint8_t* __restrict__ U, uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
+__device__ __forceinline__ void rgb24_to_yuv420p_v8(const uint8_t* __restrict__ rgb, int w, int h, int rgb_ls,
+                                                    uint8_t* __restrict__ Y, uint8_t* __restrict__ U,
+                                                    uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
   const int cw = (w + 1) >> 1, ch = (h + 1) >> 1;
   const int cx0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int cy = blockIdx.y;
@@ -153,9 +153,9 @@ rgb24_to_yuv420p_v8_kernel(const uint8_t* __restrict__ rgb, int w, int h, int rg
   *reinterpret_cast<uint32_t*>(V + (size_t)cy * ls2 + cx0) = vw;
 }
 
-__global__ void __launch_bounds__(kGlueThreads)
-gray8_to_yuv420p_v8_kernel(const uint8_t* __restrict__ g, int w, int h, int g_ls, uint8_t* __restrict__ Y,
-                           uint8_t* __restrict__ U, uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
+__device__ __forceinline__ void gray8_to_yuv420p_v8(const uint8_t* __restrict__ g, int w, int h, int g_ls,
+                                                    uint8_t* __restrict__ Y, uint8_t* __restrict__ U,
+                                                    uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
   const int cw = (w + 1) >> 1, ch = (h + 1) >> 1;
   const int cx0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int cy = blockIdx.y;
@@ -191,6 +191,55 @@ gray8_to_yuv420p_v8_kernel(const uint8_t* __restrict__ g, int w, int h, int g_ls
   *reinterpret_cast<uint32_t*>(V + (size_t)cy * ls2 + cx0) = 0x80808080u;
 }
 
+__global__ void __launch_bounds__(kGlueThreads)
+rgb24_to_yuv420p_v8_kernel(const uint8_t* __restrict__ rgb, int w, int h, int rgb_ls, uint8_t* __restrict__ Y,
+                           uint8_t* __restrict__ U, uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
+  rgb24_to_yuv420p_v8(rgb, w, h, rgb_ls, Y, U, V, ls0, ls1, ls2);
+}
+
+__global__ void __launch_bounds__(kGlueThreads)
+gray8_to_yuv420p_v8_kernel(const uint8_t* __restrict__ g, int w, int h, int g_ls, uint8_t* __restrict__ Y,
+                           uint8_t* __restrict__ U, uint8_t* __restrict__ V, int ls0, int ls1, int ls2) {
+  gray8_to_yuv420p_v8(g, w, h, g_ls, Y, U, V, ls0, ls1, ls2);
+}
+
+// Batched forms: frame f = blockIdx.z of one launch, same geometry and
+// linesizes for every frame, per-frame plane pointers in the parameter table.
+__global__ void __launch_bounds__(kGlueThreads)
+rgb24_to_yuv420p_batch_kernel(const FrameSet fs, int w, int h, int src_ls, int ls0, int ls1, int ls2, int vec) {
+  const int f = blockIdx.z;
+  if (vec) {
+    rgb24_to_yuv420p_v8(fs.src[f], w, h, src_ls, fs.y[f], fs.u[f], fs.v[f], ls0, ls1, ls2);
+  } else {
+    const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+    if (cx < (w + 1) >> 1 && cy < (h + 1) >> 1)
+      rgb_block_scalar(fs.src[f], w, h, src_ls, fs.y[f], fs.u[f], fs.v[f], ls0, ls1, ls2, cx, cy);
+  }
+}
+
+__global__ void __launch_bounds__(kGlueThreads)
+gray8_to_yuv420p_batch_kernel(const FrameSet fs, int w, int h, int src_ls, int ls0, int ls1, int ls2, int vec) {
+  const int f = blockIdx.z;
+  if (vec) {
+    gray8_to_yuv420p_v8(fs.src[f], w, h, src_ls, fs.y[f], fs.u[f], fs.v[f], ls0, ls1, ls2);
+    return;
+  }
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= (w + 1) >> 1 || cy >= (h + 1) >> 1) return;
+  constexpr int32_t ys = kYR + kYG + kYB;
+  const uint8_t* g = fs.src[f];
+  for (int dy = 0; dy < 2; ++dy) {
+    const int yy = 2 * cy + dy;
+    if (yy >= h) break;
+    for (int dx = 0; dx < 2; ++dx) {
+      const int xx = 2 * cx + dx;
+      if (xx < w) fs.y[f][(size_t)yy * ls0 + xx] = clamp8((ys * g[(size_t)yy * src_ls + xx] + (16 << 16) + (1 << 15)) >> 16);
+    }
+  }
+  fs.u[f][(size_t)cy * ls1 + cx] = 128;
+  fs.v[f][(size_t)cy * ls2 + cx] = 128;
+}
+
 // round-half-up of d * 1000 in FP32; NaN/negative -> 0; saturate at 65535.
 __device__ __forceinline__ uint16_t pack_mm(float d) {
   const float mm = __fmul_rn(d, 1000.0f);
@@ -216,6 +265,27 @@ __device__ __forceinline__ uint8_t unit_q(float x) {
 __global__ void depth_pack_u16mm_kernel(const float* __restrict__ d, size_t n, uint16_t* __restrict__ out, int vec) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   size_t i0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t done = 0;
+  if (vec) {
+    const size_t n4 = n / 4;
+    for (size_t i = i0; i < n4; i += stride) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(d) + i);
+      reinterpret_cast<uint2*>(out)[i] =
+          make_uint2((uint32_t)pack_mm(v.x) | ((uint32_t)pack_mm(v.y) << 16),
+                     (uint32_t)pack_mm(v.z) | ((uint32_t)pack_mm(v.w) << 16));
+    }
+    done = n4 * 4;
+  }
+  for (size_t i = done + i0; i < n; i += stride) out[i] = pack_mm(d[i]);
+}
+
+// Batched depth packing: frame f = blockIdx.y, n elements per frame.
+__global__ void depth_pack_u16mm_batch_kernel(const DepthSet ds, size_t n, int vec) {
+  const int f = blockIdx.y;
+  const float* __restrict__ d = ds.src[f];
+  uint16_t* __restrict__ out = ds.dst[f];
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t i0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   size_t done = 0;
   if (vec) {
     const size_t n4 = n / 4;
@@ -323,6 +393,31 @@ cudaError_t launch_depth_to_gray8(const float* d, size_t n, float dmax, uint8_t*
 
 cudaError_t launch_rgb_to_rgb24(const float* rgb, size_t n, uint8_t* out, cudaStream_t stream) {
   rgb_to_rgb24_kernel<<<grid_for(n), kGlueThreads, 0, stream>>>(rgb, n, out, aligned(rgb, 16) && aligned(out, 4));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_yuv420p_batch(bool gray, const FrameSet& fs, int nframes, int w, int h, int src_ls,
+                                 const int ls[3], cudaStream_t stream) {
+  if (nframes < 1 || nframes > kMaxBatchFrames) return cudaErrorInvalidValue;
+  bool vec = true;
+  for (int f = 0; f < nframes; ++f) vec = vec && yuv_vec_ok(fs.src[f], src_ls, fs.y[f], fs.u[f], fs.v[f], ls);
+  const int cw = (w + 1) / 2, ch = (h + 1) / 2;
+  const int xs = vec ? (cw + 3) / 4 : cw;
+  dim3 grid((xs + kGlueThreads - 1) / kGlueThreads, ch, nframes);
+  if (gray)
+    gray8_to_yuv420p_batch_kernel<<<grid, kGlueThreads, 0, stream>>>(fs, w, h, src_ls, ls[0], ls[1], ls[2], vec);
+  else
+    rgb24_to_yuv420p_batch_kernel<<<grid, kGlueThreads, 0, stream>>>(fs, w, h, src_ls, ls[0], ls[1], ls[2], vec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_depth_pack_u16mm_batch(const DepthSet& ds, int nframes, size_t n, cudaStream_t stream) {
+  if (nframes < 1 || nframes > kMaxBatchFrames) return cudaErrorInvalidValue;
+  bool vec = true;
+  for (int f = 0; f < nframes; ++f) vec = vec && aligned(ds.src[f], 16) && aligned(ds.dst[f], 8);
+  unsigned gx = grid_for(n * (size_t)nframes) / (unsigned)nframes;
+  dim3 grid(gx ? gx : 1, nframes);
+  depth_pack_u16mm_batch_kernel<<<grid, kGlueThreads, 0, stream>>>(ds, n, vec);
   return cudaGetLastError();
 }
 

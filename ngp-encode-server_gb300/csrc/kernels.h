@@ -76,6 +76,23 @@ cudaError_t launch_depth_to_gray8(const float* d, size_t n, float dmax, uint8_t*
                                   cudaStream_t stream);
 cudaError_t launch_rgb_to_rgb24(const float* rgb, size_t n, uint8_t* out, cudaStream_t stream);
 
+// Batched frame glue: up to kMaxBatchFrames frames of one geometry per
+// launch, per-frame device pointers passed by value.
+constexpr int kMaxBatchFrames = 64;
+struct FrameSet {
+  const uint8_t* src[kMaxBatchFrames];
+  uint8_t* y[kMaxBatchFrames];
+  uint8_t* u[kMaxBatchFrames];
+  uint8_t* v[kMaxBatchFrames];
+};
+struct DepthSet {
+  const float* src[kMaxBatchFrames];
+  uint16_t* dst[kMaxBatchFrames];
+};
+cudaError_t launch_yuv420p_batch(bool gray, const FrameSet& fs, int nframes, int w, int h, int src_ls,
+                                 const int ls[3], cudaStream_t stream);
+cudaError_t launch_depth_pack_u16mm_batch(const DepthSet& ds, int nframes, size_t n, cudaStream_t stream);
+
 // FP32 -> FP16 table conversion (level-major, same indexing).
 cudaError_t launch_table_to_fp16(const float2* src, __half2* dst, size_t n, cudaStream_t stream);
 

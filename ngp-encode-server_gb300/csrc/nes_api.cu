@@ -337,6 +337,56 @@ int nes_depth_pack_u16mm(const float* depth_dev, size_t n, uint16_t* out_dev, vo
   return NES_OK;
 }
 
+namespace {
+
+int yuv_batch(bool gray, int nframes, const uint8_t* const* src, int width, int height, int src_ls,
+              uint8_t* const* y, uint8_t* const* u, uint8_t* const* v, const int linesize[3], void* stream) {
+  if (nframes < 1 || nframes > NES_MAX_BATCH_FRAMES || !src || !y || !u || !v || !planes_ok(width, height, linesize))
+    return NES_EINVAL;
+  if (src_ls < (gray ? width : 3 * width)) return NES_EINVAL;
+  FrameSet fs;
+  std::memset(&fs, 0, sizeof(fs));
+  for (int f = 0; f < nframes; ++f) {
+    if (!src[f] || !y[f] || !u[f] || !v[f]) return NES_EINVAL;
+    fs.src[f] = src[f];
+    fs.y[f] = y[f];
+    fs.u[f] = u[f];
+    fs.v[f] = v[f];
+  }
+  NES_CUDA(launch_yuv420p_batch(gray, fs, nframes, width, height, src_ls, linesize,
+                                reinterpret_cast<cudaStream_t>(stream)));
+  return NES_OK;
+}
+
+}  // namespace
+
+int nes_rgb24_to_yuv420p_batch(int nframes, const uint8_t* const* rgb_dev, int width, int height, int rgb_linesize,
+                               uint8_t* const* y_dev, uint8_t* const* u_dev, uint8_t* const* v_dev,
+                               const int linesize[3], void* stream) {
+  return yuv_batch(false, nframes, rgb_dev, width, height, rgb_linesize, y_dev, u_dev, v_dev, linesize, stream);
+}
+
+int nes_gray8_to_yuv420p_batch(int nframes, const uint8_t* const* gray_dev, int width, int height,
+                               int gray_linesize, uint8_t* const* y_dev, uint8_t* const* u_dev, uint8_t* const* v_dev,
+                               const int linesize[3], void* stream) {
+  return yuv_batch(true, nframes, gray_dev, width, height, gray_linesize, y_dev, u_dev, v_dev, linesize, stream);
+}
+
+int nes_depth_pack_u16mm_batch(int nframes, const float* const* depth_dev, size_t n, uint16_t* const* out_dev,
+                               void* stream) {
+  if (nframes < 1 || nframes > NES_MAX_BATCH_FRAMES || !depth_dev || !out_dev) return NES_EINVAL;
+  DepthSet ds;
+  std::memset(&ds, 0, sizeof(ds));
+  for (int f = 0; f < nframes; ++f) {
+    if ((!depth_dev[f] || !out_dev[f]) && n) return NES_EINVAL;
+    ds.src[f] = depth_dev[f];
+    ds.dst[f] = out_dev[f];
+  }
+  if (n == 0) return NES_OK;
+  NES_CUDA(launch_depth_pack_u16mm_batch(ds, nframes, n, reinterpret_cast<cudaStream_t>(stream)));
+  return NES_OK;
+}
+
 int nes_depth_to_gray8(const float* depth_dev, size_t n, float dmax, uint8_t* out_dev, void* stream) {
   if ((!depth_dev || !out_dev) && n) return NES_EINVAL;
   if (!(dmax > 0.0f)) return NES_EINVAL;

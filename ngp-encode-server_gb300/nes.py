@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(HERE, "libnes_gb300.so")
 HEADER = os.path.normpath(os.path.join(HERE, "..", "include", "nes_gb300.h"))
 
 NES_OK = 0
+NES_MAX_BATCH_FRAMES = 64  # include/nes_gb300.h
 NES_EIO = -5
 NES_EAGAIN = -11
 NES_ENOMEM = -12
@@ -110,6 +111,11 @@ _SIGS = {
     "nes_rgb24_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
     "nes_gray8_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
     "nes_depth_pack_u16mm": (_I, [_P, _SZ, _P, _P]),
+    "nes_rgb24_to_yuv420p_batch": (_I, [_I, ctypes.POINTER(_P), _I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                        ctypes.POINTER(_P), ctypes.POINTER(_I), _P]),
+    "nes_gray8_to_yuv420p_batch": (_I, [_I, ctypes.POINTER(_P), _I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                        ctypes.POINTER(_P), ctypes.POINTER(_I), _P]),
+    "nes_depth_pack_u16mm_batch": (_I, [_I, ctypes.POINTER(_P), _SZ, ctypes.POINTER(_P), _P]),
     "nes_depth_to_gray8": (_I, [_P, _SZ, ctypes.c_float, _P, _P]),
     "nes_rgb_to_rgb24": (_I, [_P, _SZ, _P, _P]),
     "nes_scene_param": (_I, [_P, _I, _P, _SZ]),
@@ -394,6 +400,23 @@ def gray8_to_yuv420p(g_ptr, w, h, g_ls, y, u, v, ls, stream=0):
     lsa = (_I * 3)(*ls)
     check(load().nes_gray8_to_yuv420p(_P(g_ptr), w, h, g_ls, _P(y), _P(u), _P(v), lsa,
                                       _P(stream) if stream else None), "nes_gray8_to_yuv420p")
+
+
+def _ptrs(ptrs):
+    return (_P * len(ptrs))(*[_P(p) for p in ptrs])
+
+
+def yuv420p_batch(src_ptrs, w, h, src_ls, y_ptrs, u_ptrs, v_ptrs, ls, stream=0, gray=False):
+    """Batched RGB24 (or GRAY8) -> YUV420P: one launch for all frames."""
+    lsa = (_I * 3)(*ls)
+    fn = load().nes_gray8_to_yuv420p_batch if gray else load().nes_rgb24_to_yuv420p_batch
+    check(fn(len(src_ptrs), _ptrs(src_ptrs), w, h, src_ls, _ptrs(y_ptrs), _ptrs(u_ptrs), _ptrs(v_ptrs), lsa,
+             _P(stream) if stream else None), "yuv420p_batch")
+
+
+def depth_pack_u16mm_batch(d_ptrs, n, out_ptrs, stream=0):
+    check(load().nes_depth_pack_u16mm_batch(len(d_ptrs), _ptrs(d_ptrs), n, _ptrs(out_ptrs),
+                                            _P(stream) if stream else None), "nes_depth_pack_u16mm_batch")
 
 
 def depth_pack_u16mm(d_ptr, n, out_ptr, stream=0):

@@ -141,3 +141,61 @@ def test_elementwise_glue_any_alignment(cuda, nes_lib, oracle_mod, offset, extra
     # Nothing written outside [offset, offset + n).
     assert not o16.cpu().numpy()[:offset].any() and not o16.cpu().numpy()[offset + n:].any()
     assert not o8.cpu().numpy()[offset + n:].any() and not q8.cpu().numpy()[offset + n:].any()
+
+
+# Batched conversion: every frame of one launch equals the oracle's
+# single-frame result.  (1280, 720, 0) and (33, 17, 5) take the vector path,
+# (31, 9, 5) the per-sample path; frames are separate allocations.
+@pytest.mark.parametrize("w,h,pad,gray", [(1280, 720, 0, False), (33, 17, 5, False), (31, 9, 5, False),
+                                          (1280, 720, 0, True), (31, 9, 5, True)])
+def test_yuv420p_batch_matches_oracle(cuda, nes_lib, oracle_mod, w, h, pad, gray):
+    torch = cuda
+    rng = np.random.default_rng(w + 31 * h + pad)
+    nframes = 5
+    ls = nes_lib.linesizes(w)
+    ch, cw = (h + 1) // 2, (w + 1) // 2
+    src_ls = (w if gray else 3 * w) + pad
+    bufs, srcs, ys, us, vs = [], [], [], [], []
+    for f in range(nframes):
+        img = synth_frame(rng, w, h)
+        buf = np.zeros((h, src_ls), np.uint8)
+        buf[:, :(w if gray else 3 * w)] = img[:, :, 0] if gray else img.reshape(h, 3 * w)
+        bufs.append(buf)
+        srcs.append(torch.from_numpy(buf.reshape(-1)).cuda())
+        ys.append(torch.full((ls[0] * h,), 7, dtype=torch.uint8, device="cuda"))
+        us.append(torch.full((ls[1] * ch,), 7, dtype=torch.uint8, device="cuda"))
+        vs.append(torch.full((ls[2] * ch,), 7, dtype=torch.uint8, device="cuda"))
+    nes_lib.yuv420p_batch([t.data_ptr() for t in srcs], w, h, src_ls, [t.data_ptr() for t in ys],
+                          [t.data_ptr() for t in us], [t.data_ptr() for t in vs], ls, gray=gray)
+    torch.cuda.synchronize()
+    ref = oracle_mod.gray8_to_yuv420p if gray else oracle_mod.rgb24_to_yuv420p
+    for f in range(nframes):
+        oy, ou, ov = ref(bufs[f], w, h, src_ls, ls)
+        assert np.array_equal(visible(ys[f].cpu().numpy(), ls[0], w, h), visible(oy, ls[0], w, h))
+        assert np.array_equal(visible(us[f].cpu().numpy(), ls[1], cw, ch), visible(ou, ls[1], cw, ch))
+        assert np.array_equal(visible(vs[f].cpu().numpy(), ls[2], cw, ch), visible(ov, ls[2], cw, ch))
+
+
+def test_depth_pack_batch_matches_oracle(cuda, nes_lib, oracle_mod):
+    torch = cuda
+    rng = np.random.default_rng(11)
+    n = 1280 * 720 + 3  # a scalar tail after the float4 groups
+    deps = [torch.from_numpy((rng.random(n) * 70.0 - 1.0).astype(np.float32)).cuda() for _ in range(4)]
+    outs = [torch.zeros(n, dtype=torch.int16, device="cuda") for _ in range(4)]
+    nes_lib.depth_pack_u16mm_batch([d.data_ptr() for d in deps], n, [o.data_ptr() for o in outs])
+    torch.cuda.synchronize()
+    for d, o in zip(deps, outs):
+        assert np.array_equal(o.cpu().numpy().view(np.uint16), oracle_mod.depth_pack_u16mm(d.cpu().numpy()))
+
+
+def test_batch_glue_rejects_bad_arguments(cuda, nes_lib):
+    torch = cuda
+    a = torch.zeros(64 * 64 * 3, dtype=torch.uint8, device="cuda")
+    ls = nes_lib.linesizes(64)
+    for n in (0, nes_lib.NES_MAX_BATCH_FRAMES + 1):
+        p = [a.data_ptr()] * max(n, 1)
+        with pytest.raises(nes_lib.NesError):
+            nes_lib.yuv420p_batch(p[:n] if n else [], 64, 64, 192, p[:n], p[:n], p[:n], ls)
+    with pytest.raises(nes_lib.NesError):  # a null frame pointer
+        nes_lib.yuv420p_batch([a.data_ptr(), 0], 64, 64, 192, [a.data_ptr()] * 2, [a.data_ptr()] * 2,
+                              [a.data_ptr()] * 2, ls)
