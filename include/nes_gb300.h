@@ -393,6 +393,14 @@ int nes_scene_generate(uint64_t seed, uint32_t log2_table_size, float *table_out
  * colour W3 [3][64] (row-major [out][in]). */
 int nes_scene_param(nes_ctx *ctx, int which, float *host_out, size_t count);
 
+/* Replaces one scene parameter array from host memory (same `which`, count
+ * and layout as nes_scene_param), e.g. to render a refitted student's table
+ * and weights.  A tensor-core context re-derives its FP16 table, per-cell
+ * corner records and MLP weight image.  The occupancy grid is kept: call
+ * nes_rebuild_occupancy for the new field.  No counterpart in neserver, whose
+ * scene lives in the external renderer. */
+int nes_scene_set_param(nes_ctx *ctx, int which, const float *host_in, size_t count);
+
 /* Copies the 128^3 occupancy bitfield (65536 uint32 words, x-fastest). */
 int nes_occupancy(nes_ctx *ctx, uint32_t *host_bits);
 

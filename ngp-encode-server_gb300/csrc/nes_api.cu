@@ -468,6 +468,36 @@ int nes_scene_param(nes_ctx* c, int which, float* host_out, size_t count) {
   return NES_OK;
 }
 
+int nes_scene_set_param(nes_ctx* c, int which, const float* host_in, size_t count) {
+  if (!c || !host_in) return NES_EINVAL;
+  std::lock_guard<std::mutex> lock(c->mu);
+  NES_CUDA(cudaSetDevice(c->cfg.device));
+  float* dst = nullptr;
+  size_t n = 0;
+  switch (which) {
+    case 0: dst = reinterpret_cast<float*>(c->d_table32); n = (size_t)kLevels * c->scene.T * 2; break;
+    case 1: dst = c->d_weights + kOffDW1; n = kHid * kEnc; break;
+    case 2: dst = c->d_weights + kOffDW2; n = kDOut * kHid; break;
+    case 3: dst = c->d_weights + kOffCW1; n = kHid * kCIn; break;
+    case 4: dst = c->d_weights + kOffCW2; n = kHid * kHid; break;
+    case 5: dst = c->d_weights + kOffCW3; n = 3 * kHid; break;
+    default: return NES_EINVAL;
+  }
+  if (count != n) return NES_EINVAL;
+  NES_CUDA(cudaStreamSynchronize(c->stream));
+  NES_CUDA(cudaMemcpy(dst, host_in, n * sizeof(float), cudaMemcpyHostToDevice));
+  if (c->cfg.precision == NES_PREC_FP16_TC) {  // the tensor-core path's derived copies
+    if (which == 0) {
+      NES_CUDA(launch_table_to_fp16(c->d_table32, c->d_table16, (size_t)kLevels * c->scene.T, c->stream));
+      NES_CUDA(launch_build_records(c->d_table16, c->scene.T, c->scene.dense_mask, c->d_rec16, c->stream));
+    } else {
+      NES_CUDA(launch_pack_tc_weights(c->d_weights, c->d_tc_weights, c->stream));
+    }
+    NES_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return NES_OK;
+}
+
 int nes_occupancy(nes_ctx* c, uint32_t* host_bits) {
   if (!c || !host_bits) return NES_EINVAL;
   std::lock_guard<std::mutex> lock(c->mu);

@@ -111,6 +111,7 @@ _SIGS = {
     "nes_rgb24_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
     "nes_gray8_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
     "nes_depth_pack_u16mm": (_I, [_P, _SZ, _P, _P]),
+    "nes_scene_set_param": (_I, [_P, _I, _P, _SZ]),
     "nes_rgb24_to_yuv420p_batch": (_I, [_I, ctypes.POINTER(_P), _I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                         ctypes.POINTER(_P), ctypes.POINTER(_I), _P]),
     "nes_gray8_to_yuv420p_batch": (_I, [_I, ctypes.POINTER(_P), _I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
@@ -279,6 +280,11 @@ class Renderer:
         out = np.empty(count, dtype=np.float32)
         check(self.lib.nes_scene_param(self.h, which, out.ctypes.data, count), "nes_scene_param")
         return out
+
+    def set_scene_param(self, which, arr):
+        import numpy as np
+        a = np.ascontiguousarray(arr, dtype=np.float32).reshape(-1)
+        check(self.lib.nes_scene_set_param(self.h, which, a.ctypes.data, a.size), "nes_scene_set_param")
 
     def occupancy(self):
         import numpy as np

@@ -79,8 +79,8 @@ def test_batched_views_equal_single_views(renderer, cuda, nes_lib):
 
 def test_views_behind_a_large_view_equal_single_views(renderer, cuda, nes_lib):
     """A 1280x720 view first gives every march slot several rays, so the small
-    views behind it run in slots with a history (the tensor-core march keeps
-    two compositing contexts per slot); their pixels must not change."""
+    views behind it run in slots that hand over from one ray to the next;
+    their pixels must not change."""
     poses = nes_lib.shell_poses(12, 4, 1.2, 2.0)
     small = [(m, 96, 64, nes_lib.focal_from_fov(96, 100.0)) for m in nes_lib.stereo_pair(poses[3], 0.063)]
     views = [(poses[1], 1280, 720, nes_lib.focal_from_fov(1280, 90.0))] + small
@@ -157,10 +157,13 @@ def test_occupancy_matches_oracle(r32, scene0):
     assert np.all(bits == 0xFFFFFFFF)
 
 
-def test_partial_occupancy_skips_cells(nes_lib, cuda, scene0):
+@pytest.mark.parametrize("prec", ["fp32", "tc"])
+def test_partial_occupancy_skips_cells(nes_lib, cuda, scene0, prec):
     """With a threshold near the median density the grid is partial; the
-    march must skip empty cells exactly like the oracle given the same grid."""
-    r = nes_lib.Renderer(precision=nes_lib.PREC_FP32, max_pixels=64 * 64)
+    march must skip empty cells exactly like the oracle given the same grid
+    (the same sample count on both paths)."""
+    P = nes_lib.PREC_FP32 if prec == "fp32" else nes_lib.PREC_FP16_TC
+    r = nes_lib.Renderer(precision=P, max_pixels=64 * 64)
     try:
         r.rebuild_occupancy(0.37)
         bits = r.occupancy()
@@ -174,7 +177,8 @@ def test_partial_occupancy_skips_cells(nes_lib, cuda, scene0):
         W = H = 48
         f = nes_lib.focal_from_fov(W, 90.0)
         (rgb, dep), = render_gpu(r, cuda, [(M, W, H, f)])
-        orgb, odep, _ = scene0.render(M, W, H, f, occ=bits)
+        orgb, odep, osamples = scene0.render(M, W, H, f, occ=bits)
+        assert r.last_sample_count() == osamples
         assert psnr(rgb, orgb) >= PSNR_MIN
         assert np.abs(dep - odep).max() <= DEPTH_TOL
     finally:
@@ -194,3 +198,47 @@ def test_invalid_views_rejected(r32, nes_lib, cuda):
     with pytest.raises(nes_lib.NesError) as e:
         r32.render_views([big], [None], [None])
     assert e.value.code == nes_lib.NES_EINVAL
+
+
+@pytest.mark.parametrize("prec", ["fp32", "tc"])
+def test_early_termination_vs_oracle(nes_lib, oracle_mod, cuda, prec):
+    """A nearly opaque field: every weight of density W2's logit row set to
+    2.0 makes sigma ~ 200 inside the cube (median of the oracle's field), so
+    each ray stops after the sample that takes its transmittance below 1e-4
+    (tens of samples instead of hundreds).  The tensor-core march finalises
+    such a ray in its MLP thread and drops the samples its encoder produced
+    meanwhile."""
+    P = nes_lib.PREC_FP32 if prec == "fp32" else nes_lib.PREC_FP16_TC
+    W, H = 64, 48
+    M = nes_lib.shell_poses(0, 3, 1.5, 1.5)[1]
+    f = nes_lib.focal_from_fov(W, 90.0)
+    with nes_lib.Renderer(precision=P, max_pixels=4 * W * H) as r:
+        render_gpu(r, cuda, [(M, W, H, f)])
+        full_march = r.last_sample_count()
+        w2 = r.scene_param(2, 16 * 64).reshape(16, 64)
+        w2[0, :] = 2.0
+        r.set_scene_param(2, w2)
+        assert np.array_equal(r.scene_param(2, 16 * 64).reshape(16, 64), w2)
+        r.rebuild_occupancy(0.01)
+        (rgb, dep), = render_gpu(r, cuda, [(M, W, H, f)])
+        samples = r.last_sample_count()
+        occ = r.occupancy()
+    sc = oracle_mod.Scene(0, 19)
+    sc.set_param(2, w2)
+    assert sc.query(np.array([0.5, 0.5, 0.5]), np.array([0.0, 0.0, 1.0]))[0] > 20.0
+    orgb, odep, osamples = sc.render(M, W, H, f, occ=occ)
+    assert samples < full_march // 3, (samples, full_march)
+    if prec == "fp32":
+        assert samples == osamples
+    else:  # FP16 MLP: a ray's T may cross 1e-4 one sample earlier or later
+        assert abs(samples - osamples) <= 2 + osamples // 1000, (samples, osamples)
+    assert psnr(rgb, orgb) >= PSNR_MIN
+    assert np.abs(dep - odep).max() <= DEPTH_TOL
+
+
+def test_scene_set_param_rejects_bad_sizes(nes_lib, cuda):
+    with nes_lib.Renderer(precision=nes_lib.PREC_FP32, max_pixels=64) as r:
+        with pytest.raises(nes_lib.NesError):
+            r.set_scene_param(2, np.zeros(16 * 64 + 1, np.float32))
+        with pytest.raises(nes_lib.NesError):
+            r.set_scene_param(6, np.zeros(4, np.float32))
