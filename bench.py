@@ -321,6 +321,7 @@ def run_ours(args):
     if world == 1 and not args.no_extras:
         line["stereo"] = run_stereo(dev, min(args.steps, 20))
         line["serving"] = run_serving(dev, args.serve_seconds)
+        line["serving_delay_bounded"] = run_serving(dev, args.serve_seconds, max_queue_ms=100.0)
         line["glue"] = run_glue(dev, {"hbm_gbs": hbm})
         if args.train_steps > 0:
             line["training"] = run_training(dev, args.train_steps, batch=args.train_batch)
@@ -594,10 +595,12 @@ def random_walk_poses(seed, n, rmin=1.2, rmax=2.0, jitter_deg=0.5):
     return out
 
 
-def run_serving(dev, seconds):
+def run_serving(dev, seconds, max_queue_ms=0.0):
     """Serving form: open-loop Poisson arrivals, resolutions mixed uniformly
     over mono 640x360, 1280x720, 1920x1080 and stereo 2x1920x1832, random-walk
-    poses; latency = submit -> YUV + depth ready on the device."""
+    poses; latency = submit -> YUV + depth ready on the device.  With
+    max_queue_ms > 0 the server rejects a request at submit when its expected
+    pose -> YUV time exceeds that bound."""
     import threading as th
     import numpy as np
     import nes
@@ -605,7 +608,7 @@ def run_serving(dev, seconds):
     out = {}
     with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=2 * 1920 * 1832, device=dev.index) as r:
         srv = nes.Server(r, max_inflight_batches=2, max_batch_pixels=2 * 1920 * 1832,
-                         hbm_budget_bytes=80 << 30, max_pending=16)
+                         hbm_budget_bytes=80 << 30, max_pending=16, max_queue_ms=max_queue_ms)
         try:
             for rate in (90, 360, 720):
                 rng = np.random.default_rng(rate)
@@ -669,7 +672,9 @@ def run_serving(dev, seconds):
             srv.close()
     out["workload"] = ("Poisson arrivals for %.1f s per rate; mono 640x360 / 1280x720 / 1920x1080 and stereo "
                        "2x1920x1832 uniformly; random-walk poses on the r=1.2..2.0 shell (0.5 deg jitter); "
-                       "FP16 tcgen05; 2 batches in flight; latency = submit -> YUV+depth on device" % seconds)
+                       "FP16 tcgen05; 2 batches in flight; latency = submit -> YUV+depth on device; admission: "
+                       "80 GB budget, 16 pending, %s" % (seconds, "expected delay <= %g ms" % max_queue_ms
+                                                          if max_queue_ms else "no delay bound"))
     out["batches"] = st["batches"]
     out["graph_instantiations"] = st["graph_instantiations"]
     out["graph_updates"] = st["graph_updates"]

@@ -174,6 +174,9 @@ typedef struct nes_server_config {
   uint32_t max_inflight_batches; /* batches on the GPU at once (1..4) */
   uint32_t max_pending;          /* admitted requests waiting for a batch */
   int32_t use_graphs;            /* 1: CUDA graph per batch shape, 0: plain launches */
+  float max_queue_ms;            /* > 0: reject a request whose estimated pose -> YUV time
+                                  * (its pixels plus every pixel queued or in flight, at the
+                                  * measured pixel throughput) exceeds this; 0: no bound */
 } nes_server_config;
 
 typedef struct nes_request {
@@ -210,7 +213,10 @@ int nes_server_create(nes_ctx *ctx, const nes_server_config *cfg, nes_server **o
 void nes_server_destroy(nes_server *srv);
 
 /* Admits a request.  NES_EAGAIN when the budget or the pending queue is
- * full (the request is dropped and counted), NES_EINVAL for a bad request. */
+ * full, or when max_queue_ms is set and the request would wait longer (the
+ * request is dropped and counted), NES_EINVAL for a bad request.  Until the
+ * first batch has completed (no throughput estimate yet) the bound admits at
+ * most max_batch_pixels of queued and running pixels. */
 int nes_submit(nes_server *srv, const nes_request *req, uint64_t *ticket);
 
 /* Waits up to timeout_ns (< 0: forever) for the request; NES_ETIMEDOUT when

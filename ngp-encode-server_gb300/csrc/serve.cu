@@ -78,6 +78,7 @@ struct Req {
   ReqState state = ReqState::Pending;
   int status = NES_OK;
   Clock::time_point t_submit, t_done;
+  double pred_ms = 0.0;  // expected pose -> YUV time at admission (0: no estimate yet)
   uint64_t batch_id = 0;
   uint32_t batch_requests = 0, batch_views = 0;
 };
@@ -94,6 +95,7 @@ struct Slot {
   uint64_t batch_id = 0;
   std::vector<uint64_t> tickets;
   uint64_t pixels = 0;
+  Clock::time_point t_launch;
   std::map<std::string, cudaGraphExec_t> graphs;
 };
 
@@ -112,6 +114,15 @@ struct nes_server {
   std::deque<uint64_t> pending;
   std::deque<int> launch_order;  // slots in launch order (completion order)
   uint64_t next_ticket = 1, next_batch = 1;
+  // Admission by expected delay: pixels admitted but not yet batched, pixels
+  // of the batches on the GPU, and the measured service rate (pixels per ms,
+  // an exponential average over completed batches; 0 until the first).  The
+  // model leaves out host work between batches (graph updates, allocation)
+  // and batching granularity, so its predictions are scaled by the running
+  // ratio of measured to predicted latency of completed requests.
+  uint64_t pending_pixels = 0, inflight_pixels = 0;
+  double rate_px_per_ms = 0.0, delay_scale = 1.0;
+  Clock::time_point last_done;
   bool stop = false;
   nes_server_stats stats{};
   std::thread sched, comp;
@@ -241,7 +252,9 @@ void scheduler_main(nes_server* s) {
       tickets.push_back(s->pending.front());
       batch.push_back(&r);
       s->pending.pop_front();
+      s->pending_pixels -= px;
     }
+    s->inflight_pixels += pixels;
     const uint64_t bid = s->next_batch++;
     for (Req* r : batch) {
       r->state = ReqState::Running;
@@ -253,6 +266,7 @@ void scheduler_main(nes_server* s) {
     sl.batch_id = bid;
     sl.tickets = tickets;
     sl.pixels = pixels;
+    sl.t_launch = Clock::now();
     lk.unlock();
 
     ViewBatch vb;
@@ -267,6 +281,7 @@ void scheduler_main(nes_server* s) {
     s->stats.graph_instantiations += inst;
     s->stats.graph_updates += upd;
     if (rc != NES_OK) {  // publish the failure; nothing is in flight on this slot
+      s->inflight_pixels -= sl.pixels;
       for (uint64_t t : tickets) {
         Req& r = s->reqs[t];
         r.state = ReqState::Done;
@@ -300,12 +315,28 @@ void completion_main(nes_server* s) {
     if (status == NES_OK && sl.h_counters[kCtrError]) status = NES_ETIMEDOUT;
     s->stats.samples += (uint64_t)sl.h_counters[kCtrSamples] | ((uint64_t)sl.h_counters[kCtrSamples + 1] << 32);
     s->stats.pixels += sl.pixels;
+    s->inflight_pixels -= sl.pixels;
+    {  // this batch's service time: from its launch, or from the previous
+       // completion if the GPU was still busy with that one
+      const Clock::time_point from = sl.t_launch > s->last_done ? sl.t_launch : s->last_done;
+      const double ms = std::chrono::duration<double, std::milli>(now - from).count();
+      if (status == NES_OK && ms > 0.0 && sl.pixels) {
+        const double r = (double)sl.pixels / ms;
+        s->rate_px_per_ms = s->rate_px_per_ms > 0.0 ? 0.8 * s->rate_px_per_ms + 0.2 * r : r;
+      }
+      s->last_done = now;
+    }
     for (uint64_t t : sl.tickets) {
       Req& r = s->reqs[t];
       r.state = ReqState::Done;
       r.status = status;
       r.t_done = now;
       s->stats.completed++;
+      if (status == NES_OK && r.pred_ms > 0.0) {
+        const double ratio = std::chrono::duration<double, std::milli>(now - r.t_submit).count() / r.pred_ms;
+        const double sc = 0.9 * s->delay_scale + 0.1 * ratio;
+        s->delay_scale = sc < 0.5 ? 0.5 : (sc > 50.0 ? 50.0 : sc);
+      }
     }
     sl.tickets.clear();
     sl.busy = false;
@@ -342,6 +373,7 @@ void nes_server_config_default(nes_server_config* cfg) {
   cfg->max_inflight_batches = 2;
   cfg->max_pending = 256;
   cfg->use_graphs = 1;
+  cfg->max_queue_ms = 0.0f;
 }
 
 int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** out) {
@@ -349,6 +381,7 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
   *out = nullptr;
   if (cfg->max_inflight_batches < 1 || cfg->max_inflight_batches > kMaxSlots) return NES_EINVAL;
   if (cfg->max_batch_pixels == 0 || cfg->max_batch_pixels > (1u << 27) || cfg->max_pending == 0) return NES_EINVAL;
+  if (!(cfg->max_queue_ms >= 0.0f && cfg->max_queue_ms < 1e9f)) return NES_EINVAL;
   if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return NES_ENODEV;
   nes_server* s = new (std::nothrow) nes_server;
   if (!s) return NES_ENOMEM;
@@ -456,14 +489,24 @@ int nes_submit(nes_server* s, const nes_request* req, uint64_t* ticket) {
   if (px > s->cfg.max_batch_pixels) return NES_EINVAL;
   std::lock_guard<std::mutex> lk(s->mu);
   if (s->stop) return NES_EINVAL;
-  if (s->pending.size() >= s->cfg.max_pending ||
+  const double pred = s->rate_px_per_ms > 0.0
+                          ? (double)(s->pending_pixels + s->inflight_pixels + px) / s->rate_px_per_ms
+                          : 0.0;
+  // Before the first batch has completed there is no rate: keep at most one
+  // batch's worth of pixels in the system.
+  const bool late = s->cfg.max_queue_ms > 0.0f &&
+                    (s->rate_px_per_ms > 0.0 ? pred * s->delay_scale > s->cfg.max_queue_ms
+                                             : s->pending_pixels + s->inflight_pixels + px > s->cfg.max_batch_pixels);
+  if (s->pending.size() >= s->cfg.max_pending || late ||
       s->stats.budget_used_bytes + r.bytes > s->cfg.hbm_budget_bytes) {
     s->stats.rejected++;
     return NES_EAGAIN;
   }
+  s->pending_pixels += px;
   s->stats.submitted++;
   s->stats.budget_used_bytes += r.bytes;
   r.t_submit = Clock::now();
+  r.pred_ms = pred;
   const uint64_t t = s->next_ticket++;
   s->reqs.emplace(t, r);
   s->pending.push_back(t);

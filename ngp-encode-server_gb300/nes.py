@@ -67,7 +67,7 @@ class NesFrameRequest(ctypes.Structure):
 class NesServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_batch_pixels", ctypes.c_uint32),
                 ("max_inflight_batches", ctypes.c_uint32), ("max_pending", ctypes.c_uint32),
-                ("use_graphs", ctypes.c_int32)]
+                ("use_graphs", ctypes.c_int32), ("max_queue_ms", ctypes.c_float)]
 
 
 class NesRequest(ctypes.Structure):

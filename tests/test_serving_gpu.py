@@ -141,3 +141,32 @@ def test_invalid_requests(nes_lib, server):
         server.submit([left, right])  # stereo eyes must match in size
     with pytest.raises(nes_lib.NesError):
         server.submit([nes_lib.make_view(pose, 0, 64, f)])
+
+
+def test_queue_delay_bound_rejects_late_requests(nes_lib, rtc):
+    """max_queue_ms: once a batch has completed (the throughput estimate), a
+    burst of stereo 2x1920x1832 requests (~30 ms each) is admitted only while
+    the expected pose -> YUV time stays within 100 ms; without the bound the
+    same burst is admitted in full."""
+    pose = nes_lib.shell_poses(21, 1, 1.5, 1.5)[0]
+    big = views_for(nes_lib, pose, 1920, 1832, 100.0, True)
+    admitted = {}
+    for bound in (0.0, 100.0):
+        srv = nes_lib.Server(rtc, max_inflight_batches=1, max_batch_pixels=2 * 1920 * 1832,
+                             hbm_budget_bytes=8 << 30, max_pending=64, max_queue_ms=bound)
+        try:
+            t0 = srv.submit(big)
+            assert t0 is not None
+            srv.wait(t0)
+            srv.release(t0)
+            tickets = [srv.submit(big) for _ in range(8)]
+            ok = [t for t in tickets if t is not None]
+            for t in ok:
+                assert srv.wait(t).status == 0
+                srv.release(t)
+            admitted[bound] = len(ok)
+            assert srv.stats()["rejected"] == 8 - len(ok)
+        finally:
+            srv.close()
+    assert admitted[0.0] == 8
+    assert 1 <= admitted[100.0] < 8, admitted
