@@ -70,6 +70,29 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def job_time_ms(local_ms, world, device="cpu"):
+    """The whole job's timed region: the maximum of every rank's (an
+    all-reduce over the initialised process group when world > 1)."""
+    if world <= 1:
+        return float(local_ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mrays(world, pixels_per_step, steps, job_ms):
+    """Whole-job Mrays/s: every rank renders its own requests (weak scaling)."""
+    return world * pixels_per_step * steps / (job_ms / 1e3) / 1e6
+
+
+def rank_poses(rank):
+    """The request poses rank `rank` serves (each rank its own seeded set)."""
+    import nes
+    return nes.shell_poses(rank, NPOSES, RADIUS, RADIUS)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during a timed region."""
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -187,7 +210,7 @@ def run_ours(args):
     precisions = {"fp32": [nes.PREC_FP32], "tc": [nes.PREC_FP16_TC],
                   "auto": [nes.PREC_FP16_TC, nes.PREC_FP32]}[args.precision]
 
-    poses = nes.shell_poses(rank, NPOSES, RADIUS, RADIUS)  # each rank serves its own requests
+    poses = rank_poses(rank)
     focal = nes.focal_from_fov(W, FOV)
     views = [nes.make_view(m, W, H, focal) for m in poses]
     ls = nes.linesizes(W)
@@ -240,13 +263,9 @@ def run_ours(args):
                     samples.append(r.last_sample_count())
                 torch.cuda.synchronize()
             step_ms = [a.elapsed_time(b) for a, b in ev]
-            total_ms = sum(step_ms)
-            if world > 1:
-                t = torch.tensor([total_ms], device=dev)
-                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-                total_ms = float(t.item())
+            total_ms = job_time_ms(sum(step_ms), world, dev)
             res = {"total_ms": total_ms, "ms_per_step": total_ms / args.steps,
-                   "mrays": world * W * H * args.steps / (total_ms / 1e3) / 1e6,
+                   "mrays": job_mrays(world, W * H, args.steps, total_ms),
                    "march_ms": statistics.mean(march_ms), "raygen_ms": statistics.mean(raygen_ms),
                    "samples_per_step": statistics.mean(samples), "clocks": clk.summary()}
 

@@ -1,0 +1,59 @@
+"""The N > 1 bench path on CPU: two `gloo` ranks, each timing its own
+requests.  The job's time is the maximum over ranks and its throughput the
+pixels of all ranks over that time; each rank serves its own pose set."""
+import os
+import socket
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, q):
+    import torch.distributed as dist
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, os.path.join(REPO, "ngp-encode-server_gb300"))
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    import bench
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    try:
+        r, w, local = bench.dist_env()
+        local_ms = 100.0 * (rank + 1)  # rank 1 is the slower one
+        job = bench.job_time_ms(local_ms, w)
+        poses = bench.rank_poses(r)
+        q.put((r, w, local, job, bench.job_mrays(w, 1920 * 1080, 10, job), [list(p) for p in poses[:2]]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_time_and_throughput():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (r0, w0, l0, job0, mr0, poses0), (r1, w1, l1, job1, mr1, poses1) = out
+    assert (r0, r1, w0, w1, l0, l1) == (0, 1, 2, 2, 0, 1)
+    assert job0 == job1 == pytest.approx(200.0)        # max over ranks
+    assert mr0 == mr1 == pytest.approx(2 * 1920 * 1080 * 10 / 0.2 / 1e6)  # all ranks' pixels over that time
+    assert poses0 != poses1                             # each rank serves its own requests
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, REPO)
+    import bench
+    assert bench.job_time_ms(12.5, 1) == 12.5
+    assert bench.job_mrays(1, 100, 4, 1000.0) == pytest.approx(400 / 1.0 / 1e6)
