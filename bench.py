@@ -43,6 +43,9 @@ GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
 # dram__bytes_read.sum + dram__bytes_write.sum of one full 1920x1080 march
 # launch, from the ncu captures summarised in profiles/march_*_1080p.md.
 DRAM_BYTES_PER_LAUNCH = {"fp16": 117.358e6 + 13.557e6, "fp32": 73.651e6 + 7.437e6}
+# The tensor-core march's binding unit, from the same capture: L1 data-pipe
+# (LSU) wavefronts as a fraction of their peak rate, averaged over SMs.
+L1_WAVEFRONT_FRAC = {"fp16": 0.685}
 WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
 
 
@@ -325,6 +328,7 @@ def run_ours(args):
                                      "by L1/L2",
                      "limiter": "hash-table gathers: L1 data pipe at 68-72% of its wavefront rate, ALU 41%, "
                                 "tensor pipe 11% (ncu, profiles/march_tc_1080p.md)",
+                     "l1_wavefront_frac": L1_WAVEFRONT_FRAC.get(kind),
                      "kernel": "march", "peak_source": src + " bf16 sustained",
                      "march_ms": round(head["march_ms"], 3), "raygen_ms": round(head["raygen_ms"], 4),
                      "samples_per_step": int(head["samples_per_step"]),
