@@ -787,6 +787,27 @@ __global__ void pack_bt_images_kernel(const float* __restrict__ w, uint8_t* __re
 
 __device__ __forceinline__ uint32_t f2u(float v) { return __float_as_uint(v); }
 
+// Staging of features f..f+3 (f % 4 == 0) of this thread's record.  The four
+// lanes of a quad hold four consecutive records; a 4x4 transpose inside the
+// quad (two shuffle stages) gives lane q feature f+q of all four records,
+// which is one 16-byte row of the canonical K-major layout: one vector store
+// instead of four scalar ones.  Every lane of the warp must call it.
+__device__ __forceinline__ void stage4(float* arr, int F, uint32_t s, int f, float a0, float a1, float a2, float a3,
+                                       bool stage) {
+  const uint32_t q = threadIdx.x & 3u;
+  const bool odd = q & 1u, hi = q & 2u;
+  float t = __shfl_xor_sync(0xffffffffu, odd ? a0 : a1, 1);
+  if (odd) a0 = t; else a1 = t;
+  t = __shfl_xor_sync(0xffffffffu, odd ? a2 : a3, 1);
+  if (odd) a2 = t; else a3 = t;
+  t = __shfl_xor_sync(0xffffffffu, hi ? a0 : a2, 2);
+  if (hi) a0 = t; else a2 = t;
+  t = __shfl_xor_sync(0xffffffffu, hi ? a1 : a3, 2);
+  if (hi) a1 = t; else a3 = t;
+  if (stage)
+    *reinterpret_cast<float4*>(stage_row(arr, F, s & ~3u) + soff(f + (int)q)) = make_float4(a0, a1, a2, a3);
+}
+
 __global__ void __launch_bounds__(kBtThreads, 1)
 backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t count,
                    const TrainRay* __restrict__ rays, const DevScene sc, const uint8_t* __restrict__ images,
@@ -869,30 +890,30 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
           for (int k = 0; k < kEnc; ++k) enc[k] = 0.0f;
         }
 #pragma unroll
-        for (int k = 0; k < kEnc; ++k) {
-          if (stage) stage_row(st.enc, kEnc, s)[soff(k)] = enc[k];
-          u[k] = f2u(enc[k]);
-        }
+        for (int k = 0; k < kEnc; ++k) u[k] = f2u(enc[k]);
         tc::tmem_st32_nowait(a_row, u);
+#pragma unroll
+        for (int k = 0; k < kEnc; k += 4) stage4(st.enc, kEnc, s, k, enc[k], enc[k + 1], enc[k + 2], enc[k + 3], stage);
       }
       if (!mma(0)) break;
       uint64_t m_h1 = 0, m_g1 = 0, m_g2 = 0;
       // ReLU of D[:, :64] -> staging, mask, next A.
-      auto relu64 = [&](float* r_act, uint64_t& m) {
+      auto relu64 = [&](float* act, uint64_t& m) {
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
           tc::tmem_ld32(d_row + 32 * c, v);
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const float a = valid ? fmaxf(v[j], 0.0f) : 0.0f;
-            m |= (uint64_t)(a > 0.0f) << (32 * c + j);
-            if (stage) r_act[soff(32 * c + j)] = a;
-            u[j] = f2u(a);
+            v[j] = valid ? fmaxf(v[j], 0.0f) : 0.0f;
+            m |= (uint64_t)(v[j] > 0.0f) << (32 * c + j);
+            u[j] = f2u(v[j]);
           }
           tc::tmem_st32_nowait(a_row + 32 * c, u);
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) stage4(act, kHid, s, 32 * c + j, v[j], v[j + 1], v[j + 2], v[j + 3], stage);
         }
       };
-      relu64(stage_row(st.h1, kHid, s), m_h1);
+      relu64(st.h1, m_h1);
       if (!mma(1)) break;
       float sigma;
       {
@@ -907,16 +928,17 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
         cin[31] = 0.0f;
 #pragma unroll
         for (int k = 0; k < kCIn; ++k) {
-          const float c = valid ? cin[k] : 0.0f;
-          if (stage) stage_row(st.cin, kCIn, s)[soff(k)] = c;
-          u[k] = f2u(c);
+          cin[k] = valid ? cin[k] : 0.0f;
+          u[k] = f2u(cin[k]);
         }
         tc::tmem_st32_nowait(a_row, u);
+#pragma unroll
+        for (int k = 0; k < kCIn; k += 4) stage4(st.cin, kCIn, s, k, cin[k], cin[k + 1], cin[k + 2], cin[k + 3], stage);
       }
       if (!mma(2)) break;
-      relu64(stage_row(st.g1, kHid, s), m_g1);
+      relu64(st.g1, m_g1);
       if (!mma(3)) break;
-      relu64(stage_row(st.g2, kHid, s), m_g2);
+      relu64(st.g2, m_g2);
       if (!mma(4)) break;
       // ---- backward ----
       {
@@ -927,46 +949,47 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
         uint32_t w16[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) w16[k] = k < 3 ? f2u(dl[k]) : 0u;
-#pragma unroll
-        for (int k = 0; k < kFDlog; ++k)
-          if (stage) stage_row(st.dlog, kFDlog, s)[soff(k)] = k < 3 ? dl[k] : 0.0f;
         tc::tmem_st16_nowait(a_row, w16);
+        stage4(st.dlog, kFDlog, s, 0, dl[0], dl[1], dl[2], 0.0f, stage);
+        stage4(st.dlog, kFDlog, s, 4, 0.0f, 0.0f, 0.0f, 0.0f, stage);
       }
       // Masked D[:, :64] -> staging, next A.
-      auto mask64 = [&](float* r_d, uint64_t m) {
+      auto mask64 = [&](float* delta, uint64_t m) {
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
           tc::tmem_ld32(d_row + 32 * c, v);
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const float d = ((m >> (32 * c + j)) & 1u) ? v[j] : 0.0f;
-            if (stage) r_d[soff(32 * c + j)] = d;
-            u[j] = f2u(d);
+            v[j] = ((m >> (32 * c + j)) & 1u) ? v[j] : 0.0f;
+            u[j] = f2u(v[j]);
           }
           tc::tmem_st32_nowait(a_row + 32 * c, u);
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) stage4(delta, kHid, s, 32 * c + j, v[j], v[j + 1], v[j + 2], v[j + 3], stage);
         }
       };
       if (!mma(5)) break;
-      mask64(stage_row(st.dg2, kHid, s), m_g2);
+      mask64(st.dg2, m_g2);
       if (!mma(6)) break;
-      mask64(stage_row(st.dg1, kHid, s), m_g1);
+      mask64(st.dg1, m_g1);
       if (!mma(7)) break;
       {
         float geo[16];
         tc::tmem_ld16(d_row, reinterpret_cast<float(&)[16]>(geo));
         uint32_t w16[16];
-        const float d0 = q.dsigma * sigma;
-        w16[0] = f2u(d0);
-        if (stage) stage_row(st.dout, kDOut, s)[soff(0)] = d0;
+        float dout[16];
+        dout[0] = q.dsigma * sigma;
 #pragma unroll
-        for (int m = 0; m < 15; ++m) {
-          w16[1 + m] = f2u(geo[m]);
-          if (stage) stage_row(st.dout, kDOut, s)[soff(1 + m)] = geo[m];
-        }
+        for (int m = 0; m < 15; ++m) dout[1 + m] = geo[m];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) w16[m] = f2u(dout[m]);
         tc::tmem_st16_nowait(a_row, w16);
+#pragma unroll
+        for (int m = 0; m < kDOut; m += 4)
+          stage4(st.dout, kDOut, s, m, dout[m], dout[m + 1], dout[m + 2], dout[m + 3], stage);
       }
       if (!mma(8)) break;
-      mask64(stage_row(st.dh1, kHid, s), m_h1);
+      mask64(st.dh1, m_h1);
       if (!mma(9)) break;
       tc::tmem_ld32(d_row, v);  // denc
       // The next tile's first product overwrites D: its sync follows these reads.
