@@ -242,3 +242,27 @@ def test_scene_set_param_rejects_bad_sizes(nes_lib, cuda):
             r.set_scene_param(2, np.zeros(16 * 64 + 1, np.float32))
         with pytest.raises(nes_lib.NesError):
             r.set_scene_param(6, np.zeros(4, np.float32))
+
+
+def test_scene_loaded_into_tensor_core_context(nes_lib, cuda):
+    """nes_scene_set_param on a tensor-core context rebuilds its FP16 table,
+    per-cell corner records and MMA weight image: seed 1's table and weights
+    loaded into a seed-0 context render like a seed-1 context (same sample
+    count, spec tolerances against the FP32 render)."""
+    table, w = nes_lib.scene_generate(1, 19)
+    blocks = {1: w[0:2048], 2: w[2048:3072], 3: w[3072:5120], 4: w[5120:9216], 5: w[9216:9408]}
+    M = nes_lib.shell_poses(3, 1, 1.3, 1.3)[0]
+    W, H = 96, 64
+    f = nes_lib.focal_from_fov(W, 90.0)
+    with nes_lib.Renderer(precision=nes_lib.PREC_FP16_TC, seed=0, max_pixels=W * H) as tc, \
+            nes_lib.Renderer(precision=nes_lib.PREC_FP32, seed=1, max_pixels=W * H) as ref:
+        tc.set_scene_param(0, table)
+        for i, b in blocks.items():
+            tc.set_scene_param(i, b)
+        tc.rebuild_occupancy(0.01)
+        assert np.array_equal(tc.occupancy(), ref.occupancy())
+        (a, da), = render_gpu(tc, cuda, [(M, W, H, f)])
+        (b, db), = render_gpu(ref, cuda, [(M, W, H, f)])
+        assert tc.last_sample_count() == ref.last_sample_count()
+    assert psnr(a, b) >= PSNR_MIN
+    assert np.abs(da - db).max() <= DEPTH_TOL
