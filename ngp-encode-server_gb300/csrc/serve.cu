@@ -123,6 +123,10 @@ struct nes_server {
   uint64_t pending_pixels = 0, inflight_pixels = 0;
   double rate_px_per_ms = 0.0, delay_scale = 1.0;
   Clock::time_point last_done;
+  // Batch shapes seen so far (scheduler thread only): a shape is launched
+  // directly the first time and captured as a graph once it recurs, so
+  // one-off mixes of resolutions cost no graph instantiation.
+  std::unordered_map<std::string, uint32_t> shape_seen;
   bool stop = false;
   nes_server_stats stats{};
   std::thread sched, comp;
@@ -166,12 +170,21 @@ std::string shape_key(const std::vector<Req*>& reqs) {
   return k;
 }
 
-// Launches a batch: plain launches, or capture + instantiate/update + replay.
-// Runs outside the server lock; graph counters go to *inst / *upd.
+// Launches a batch: plain launches (graphs off, or a shape's first
+// occurrence), or capture + instantiate/update + replay.  Runs outside the
+// server lock (the scheduler thread is its only caller); graph counters go to
+// *inst / *upd.
 int launch_batch(nes_server* s, Slot& sl, const ViewBatch& vb, const std::vector<Req*>& reqs, uint64_t* inst,
                  uint64_t* upd) {
   for (Req* r : reqs) SRV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&r->dev), r->bytes, sl.st));
-  if (!s->cfg.use_graphs) {
+  const std::string key = shape_key(reqs);
+  if (s->shape_seen.size() > 4096) s->shape_seen.clear();  // bounded memory for endless mixes
+  const uint32_t seen = ++s->shape_seen[key];
+  if (sl.graphs.size() > 256) {  // likewise for the executable graphs of this slot
+    for (auto& kv : sl.graphs) cudaGraphExecDestroy(kv.second);
+    sl.graphs.clear();
+  }
+  if (!s->cfg.use_graphs || (seen < 2 && sl.graphs.find(key) == sl.graphs.end())) {
     const int rc = enqueue_batch(s, sl, vb, reqs);
     if (rc != NES_OK) return rc;
   } else {
@@ -183,7 +196,6 @@ int launch_batch(nes_server* s, Slot& sl, const ViewBatch& vb, const std::vector
       if (g) cudaGraphDestroy(g);
       return rc != NES_OK ? rc : NES_EIO;
     }
-    const std::string key = shape_key(reqs);
     auto it = sl.graphs.find(key);
     bool ok = false;
     if (it != sl.graphs.end()) {

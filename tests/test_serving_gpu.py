@@ -80,10 +80,13 @@ def test_matches_synchronous_pose_to_yuv(nes_lib, server, rtc, cuda):
 
 
 def test_graph_reused_per_batch_shape(nes_lib, server):
-    pose = nes_lib.shell_poses(4, 3, 1.2, 2.0)
+    """A batch shape is launched directly on its first occurrence and
+    captured once it recurs: four batches of one shape take at most one
+    instantiation and at least two updates."""
+    pose = nes_lib.shell_poses(4, 4, 1.2, 2.0)
     before = server.stats()
     ts = []
-    for i in range(3):  # one request at a time: same shape each batch
+    for i in range(4):  # one request at a time: same shape each batch
         t = server.submit(views_for(nes_lib, pose[i], 96, 64, 90.0, False))
         server.wait(t)
         ts.append(t)
