@@ -42,10 +42,10 @@ FLOP_PER_SAMPLE = 18688          # 2 x 9,344 MLP multiply-adds
 GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
 # dram__bytes_read.sum + dram__bytes_write.sum of one full 1920x1080 march
 # launch, from the ncu captures summarised in profiles/march_*_1080p.md.
-DRAM_BYTES_PER_LAUNCH = {"fp16": 117.358e6 + 13.557e6, "fp32": 73.651e6 + 7.437e6}
+DRAM_BYTES_PER_LAUNCH = {"fp16": 2815.030e6 + 18.675e6, "fp32": 73.651e6 + 7.437e6}
 # The tensor-core march's binding unit, from the same capture: L1 data-pipe
 # (LSU) wavefronts as a fraction of their peak rate, averaged over SMs.
-L1_WAVEFRONT_FRAC = {"fp16": 0.685}
+L1_WAVEFRONT_FRAC = {"fp16": 0.694}
 WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
 
 
@@ -323,10 +323,10 @@ def run_ours(args):
         "roofline": {"bound": "tensor", "achieved": round(achieved, 3), "peak": tf_sust, "unit": "TFLOP/s",
                      "frac": round(achieved / tf_sust, 5),
                      "traffic": DRAM_BYTES_PER_LAUNCH[kind] if (W, H) == (1920, 1080) else None,
-                     "traffic_note": "DRAM bytes per launch (ncu); the FP16 table (32 MiB) and the level 0-6 "
-                                     "corner records (70 MB) stay in L2, so the 512 B/sample gathers are served "
-                                     "by L1/L2",
-                     "limiter": "hash-table gathers: L1 data pipe at 68-72% of its wavefront rate, ALU 41%, "
+                     "traffic_note": "DRAM bytes per launch (ncu); the FP16 table (32 MiB) and the corner "
+                                     "records of levels 0-6 (70 MB) stay in L2, those of levels 7-9 (1.23 GB) "
+                                     "come from HBM; the 512 B/sample of gathers are served mostly by L1/L2",
+                     "limiter": "hash-table gathers: L1 data pipe at 69-73% of its wavefront rate, ALU 40%, "
                                 "tensor pipe 11% (ncu, profiles/march_tc_1080p.md)",
                      "l1_wavefront_frac": L1_WAVEFRONT_FRAC.get(kind),
                      "kernel": "march", "peak_source": src + " bf16 sustained",

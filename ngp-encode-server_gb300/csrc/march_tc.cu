@@ -189,7 +189,7 @@ __device__ __forceinline__ uint32_t encode_level(const __half2* __restrict__ tab
 __device__ __forceinline__ void encode_all(const __half2* __restrict__ table, const uint4* __restrict__ rec,
                                            uint32_t T, uint32_t dense_mask, const float3& x, bool has,
                                            uint32_t taddr) {
-  static_assert(kRecLevels == 7, "encode_all reads levels 0..6 from the records");
+  static_assert(kRecLevels == 10, "encode_all reads levels 0..9 from the records");
   uint32_t f[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) f[k] = 0u;
@@ -201,9 +201,9 @@ __device__ __forceinline__ void encode_all(const __half2* __restrict__ table, co
     f[4] = encode_level_rec<4>(rec, x);
     f[5] = encode_level_rec<5>(rec, x);
     f[6] = encode_level_rec<6>(rec, x);
-    f[7] = encode_level<7>(table, T, dense_mask, x);
-    f[8] = encode_level<8>(table, T, dense_mask, x);
-    f[9] = encode_level<9>(table, T, dense_mask, x);
+    f[7] = encode_level_rec<7>(rec, x);
+    f[8] = encode_level_rec<8>(rec, x);
+    f[9] = encode_level_rec<9>(rec, x);
     f[10] = encode_level<10>(table, T, dense_mask, x);
     f[11] = encode_level<11>(table, T, dense_mask, x);
     f[12] = encode_level<12>(table, T, dense_mask, x);

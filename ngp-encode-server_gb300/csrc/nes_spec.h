@@ -36,15 +36,15 @@ NES_HD constexpr int level_res(int l) {
 
 // Levels 0..kRecLevels-1 are also stored as per-cell records of their 8
 // corner entries for the tensor-core march: cells of level l start at
-// rec_cell_offset(l) (N_0^3 + ... + N_{l-1}^3); 2,190,575 cells, 70 MB.
-constexpr int kRecLevels = 7;
+// rec_cell_offset(l) (N_0^3 + ... + N_{l-1}^3); 40,712,464 cells, 1.30 GB.
+constexpr int kRecLevels = 10;
 NES_HD constexpr uint32_t rec_cell_offset(int l) {
   uint32_t o = 0;
   for (int j = 0; j < l; ++j) o += (uint32_t)level_res(j) * (uint32_t)level_res(j) * (uint32_t)level_res(j);
   return o;
 }
 constexpr uint32_t kRecCells = rec_cell_offset(kRecLevels);
-static_assert(kRecCells == 2190575u, "record cells of levels 0..6");
+static_assert(kRecCells == 40712464u, "record cells of levels 0..9");
 
 // Spatial-hash primes (Instant-NGP paper, Sec. 3).
 constexpr uint32_t kPrime1 = 2654435761u;
