@@ -49,6 +49,31 @@ def test_glue_rejects_bad_arguments_without_gpu(nes_lib):
     assert lib.nes_depth_pack_u16mm(None, 0, None, None) == nes_lib.NES_OK
 
 
+def test_batched_glue_and_set_param_reject_bad_arguments_without_gpu(nes_lib):
+    """The batched frame glue and nes_scene_set_param validate before any
+    CUDA call: frame counts outside 1..NES_MAX_BATCH_FRAMES, null pointer
+    arrays or frames, bad geometry, a null context."""
+    lib = nes_lib.load()
+    ls = (ctypes.c_int * 3)(64, 32, 32)
+    dummy = ctypes.c_void_p(0x1000)
+    one = (ctypes.c_void_p * 1)(dummy)
+    many = (ctypes.c_void_p * 65)(*([dummy] * 65))
+    for fn in (lib.nes_rgb24_to_yuv420p_batch, lib.nes_gray8_to_yuv420p_batch):
+        assert fn(0, one, 64, 64, 192, one, one, one, ls, None) == nes_lib.NES_EINVAL
+        assert fn(nes_lib.NES_MAX_BATCH_FRAMES + 1, many, 64, 64, 192, many, many, many, ls, None) == nes_lib.NES_EINVAL
+        assert fn(1, None, 64, 64, 192, one, one, one, ls, None) == nes_lib.NES_EINVAL
+        assert fn(1, one, 0, 64, 192, one, one, one, ls, None) == nes_lib.NES_EINVAL
+        null_frame = (ctypes.c_void_p * 1)(None)
+        assert fn(1, null_frame, 64, 64, 192, one, one, one, ls, None) == nes_lib.NES_EINVAL
+    assert lib.nes_rgb24_to_yuv420p_batch(1, one, 64, 64, 100, one, one, one, ls, None) == nes_lib.NES_EINVAL  # < 3w
+    assert lib.nes_depth_pack_u16mm_batch(0, one, 10, one, None) == nes_lib.NES_EINVAL
+    assert lib.nes_depth_pack_u16mm_batch(65, many, 10, many, None) == nes_lib.NES_EINVAL
+    assert lib.nes_depth_pack_u16mm_batch(1, None, 10, one, None) == nes_lib.NES_EINVAL
+    assert lib.nes_depth_pack_u16mm_batch(1, one, 0, one, None) == nes_lib.NES_OK  # nothing to do
+    buf = np.zeros(4, np.float32)
+    assert lib.nes_scene_set_param(None, 1, buf.ctypes.data, 4) == nes_lib.NES_EINVAL
+
+
 def test_create_validates_config(nes_lib):
     lib = nes_lib.load()
     h = ctypes.c_void_p()
