@@ -201,3 +201,19 @@ def test_oracle_matches_golden_yuv(oracle_mod):
     gy, gu, gv = oracle_mod.gray8_to_yuv420p(g["gray"], w, h, w, ls)
     assert np.array_equal(gy, g["gy"]) and np.array_equal(gu, g["gu"])
     assert np.array_equal(oracle_mod.depth_pack_u16mm(g["depth"]), g["depth_mm"])
+
+
+def test_fp32_cpu_render_matches_fp64_oracle(scene0, nes_lib):
+    """The plain FP32 CPU render (the bench's CPU baseline) evaluates the same
+    samples as the FP64 oracle and agrees with it within the spec
+    tolerances (PSNR >= 45 dB, max |delta depth| <= 1e-3)."""
+    import numpy as np
+    import oracle
+    M = nes_lib.shell_poses(0, 3, 1.5, 1.5)[2]
+    W, H = 32, 24
+    f = nes_lib.focal_from_fov(W, 90.0)
+    rgb64, dep64, n64 = scene0.render(M, W, H, f)
+    rgb32, dep32, n32 = scene0.render_f32(M, W, H, f)
+    assert n32 == n64 > 0
+    assert oracle.psnr(rgb32.astype(np.float64), rgb64) >= 45.0
+    assert np.abs(dep32.astype(np.float64) - dep64).max() <= 1e-3
