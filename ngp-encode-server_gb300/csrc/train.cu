@@ -727,8 +727,75 @@ dw_tc_kernel(Staging st, uint32_t ntiles, float* __restrict__ dw, uint32_t* __re
 constexpr int kBtGroups = 4;
 constexpr int kBtThreads = 128 * kBtGroups;
 constexpr uint32_t kBtColsPerGroup = 128;  // A: 64 columns, D: 64 columns
+
+// Hash-grid scatter-add of one record's encoding gradient,
+// dtable[l][corner] += w_corner * denc[2l..2l+1].  Every lane of the warp
+// calls it (valid = false for a lane without a record).  A warp's records
+// are consecutive samples of one or two rays, so at the coarse levels runs
+// of neighbouring lanes share a cell: levels 0..kAggLevels-1 sum each run's
+// corner gradients with shuffles and add them with one atomic per run.
 constexpr int kAggLevels = 7;  // levels whose scatter-add is warp-aggregated (N <= 111)
 static_assert(level_res(kAggLevels - 1) < 128, "cell key packs 7 bits per coordinate");
+
+__device__ __forceinline__ void scatter_add_levels(float2* __restrict__ gtable, const DevScene& sc, float3 x,
+                                                   const float (&denc)[kEnc], bool valid, uint32_t lane) {
+#pragma unroll 1
+  for (int l = 0; l < kLevels; ++l) {
+    const int N = level_res(l);
+    const LevelCell c = level_cell(x, N);
+    uint32_t idx[8];
+    corner_indices(c, N, (sc.dense_mask >> l) & 1u, sc.T, idx);
+    float w[8];
+    corner_weights(c, w);
+    float2* gt = gtable + (size_t)l * sc.T;
+    float d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kLevels; ++k)
+      if (k == l) {
+        d0 = denc[2 * k];
+        d1 = denc[2 * k + 1];
+      }
+    if (l >= kAggLevels) {
+      if (valid)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
+      continue;
+    }
+    // Runs of lanes with the same cell (invalid lanes form runs of their
+    // own and add nothing).  N <= 111 here: 7 bits per coordinate.
+    const uint32_t key = valid ? (c.ix | (c.iy << 7) | (c.iz << 14)) : (0x80000000u | lane);
+    const uint32_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
+    const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != key);
+    if (heads == 0xffffffffu) {  // no lane shares its cell
+      if (valid)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
+      continue;
+    }
+    // Step o adds the partial sum of lane + o when no run starts in
+    // (lane, lane + o]; afterwards each run's first lane holds its total.
+    uint32_t take = 0;
+#pragma unroll
+    for (int o = 1, b = 0; o < 32; o <<= 1, ++b) {
+      const uint32_t span = (uint32_t)(((1ull << o) - 1ull) << (lane + 1));  // lanes lane+1 .. lane+o
+      if (lane + o < 32u && (heads & span) == 0u) take |= 1u << b;
+    }
+    const bool head = (heads >> lane) & 1u;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float a0 = w[k] * d0, a1 = w[k] * d1;
+#pragma unroll
+      for (int o = 1, b = 0; o < 32; o <<= 1, ++b) {
+        const float p0 = __shfl_down_sync(0xffffffffu, a0, o), p1 = __shfl_down_sync(0xffffffffu, a1, o);
+        if ((take >> b) & 1u) {
+          a0 += p0;
+          a1 += p1;
+        }
+      }
+      if (valid && head) atomicAdd(gt + idx[k], make_float2(a0, a1));
+    }
+  }
+}
 
 // Weight images, [N][K] K-major, no swizzle, FP32 bits read as TF32: core
 // matrices of 8 rows x 4 elements (16 B rows, 128 B each), K-adjacent at
@@ -993,67 +1060,7 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
       if (!mma(9)) break;
       tc::tmem_ld32(d_row, v);  // denc
       // The next tile's first product overwrites D: its sync follows these reads.
-      // Hash-grid scatter-add.  A warp's 32 records are consecutive samples
-      // of one or two rays, so at the coarse levels runs of neighbouring
-      // lanes share a cell: levels 0..kAggLevels-1 sum each run's corner
-      // gradients with shuffles and add them with one atomic per run.
-      const uint32_t lane = (uint32_t)(tid & 31);
-#pragma unroll 1
-      for (int l = 0; l < kLevels; ++l) {
-        const int N = level_res(l);
-        const LevelCell c = level_cell(x, N);
-        uint32_t idx[8];
-        corner_indices(c, N, (sc.dense_mask >> l) & 1u, sc.T, idx);
-        float w[8];
-        corner_weights(c, w);
-        float2* gt = gtable + (size_t)l * sc.T;
-        float d0 = 0.0f, d1 = 0.0f;
-#pragma unroll
-        for (int k = 0; k < kLevels; ++k)
-          if (k == l) {
-            d0 = v[2 * k];
-            d1 = v[2 * k + 1];
-          }
-        if (l >= kAggLevels) {
-          if (valid)
-#pragma unroll
-            for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
-          continue;
-        }
-        // Runs of lanes with the same cell (invalid lanes form runs of their
-        // own and add nothing).  N <= 111 here: 7 bits per coordinate.
-        const uint32_t key = valid ? (c.ix | (c.iy << 7) | (c.iz << 14)) : (0x80000000u | lane);
-        const uint32_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
-        const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != key);
-        if (heads == 0xffffffffu) {  // no lane shares its cell
-          if (valid)
-#pragma unroll
-            for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
-          continue;
-        }
-        // Step o adds the partial sum of lane + o when no run starts in
-        // (lane, lane + o]; afterwards each run's first lane holds its total.
-        uint32_t take = 0;
-#pragma unroll
-        for (int o = 1, b = 0; o < 32; o <<= 1, ++b) {
-          const uint32_t span = (uint32_t)(((1ull << o) - 1ull) << (lane + 1));  // lanes lane+1 .. lane+o
-          if (lane + o < 32u && (heads & span) == 0u) take |= 1u << b;
-        }
-        const bool head = (heads >> lane) & 1u;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          float a0 = w[k] * d0, a1 = w[k] * d1;
-#pragma unroll
-          for (int o = 1, b = 0; o < 32; o <<= 1, ++b) {
-            const float p0 = __shfl_down_sync(0xffffffffu, a0, o), p1 = __shfl_down_sync(0xffffffffu, a1, o);
-            if ((take >> b) & 1u) {
-              a0 += p0;
-              a1 += p1;
-            }
-          }
-          if (valid && head) atomicAdd(gt + idx[k], make_float2(a0, a1));
-        }
-      }
+      scatter_add_levels(gtable, sc, x, v, valid, (uint32_t)(tid & 31));
     }
   }
   if (fail || !ok) atomicExch(err, kErrTimeout);
