@@ -170,7 +170,7 @@ typedef struct nes_server nes_server;
 
 typedef struct nes_server_config {
   uint64_t hbm_budget_bytes;     /* batch scratch + outputs of admitted requests */
-  uint32_t max_batch_pixels;     /* pixels per batch (sum over its views) */
+  uint32_t max_batch_pixels;     /* pixels per batch (sum over its views), 64..2^27 */
   uint32_t max_inflight_batches; /* batches on the GPU at once (1..4) */
   uint32_t max_pending;          /* admitted requests waiting for a batch */
   int32_t use_graphs;            /* 1: CUDA graph per batch shape, 0: plain launches */
@@ -214,7 +214,10 @@ void nes_server_destroy(nes_server *srv);
 
 /* Admits a request.  NES_EAGAIN when the budget or the pending queue is
  * full, or when max_queue_ms is set and the request would wait longer (the
- * request is dropped and counted), NES_EINVAL for a bad request.  Until the
+ * request is dropped and counted), NES_EINVAL for a bad request (a view
+ * that nes_render_views would reject, stereo eyes of different sizes, more
+ * than max_batch_pixels pixels): it is refused here and never reaches a
+ * batch, so it cannot fail the requests batched with it.  Until the
  * first batch has completed (no throughput estimate yet) the bound admits at
  * most max_batch_pixels of queued and running pixels. */
 int nes_submit(nes_server *srv, const nes_request *req, uint64_t *ticket);

@@ -45,6 +45,10 @@ struct nes_ctx {
 
 namespace nes {
 
+// A view the renderer accepts: 1..16384 pixels on each side, a finite
+// positive focal length and a finite pose matrix.
+bool view_ok(const nes_view& v);
+
 // Validates views and fills the kernel-side batch descriptor.  *pixels
 // receives the batch's real pixel count.  NES_EINVAL on a bad view, more
 // than kMaxViews views, or more than max_pixels pixels.

@@ -31,14 +31,6 @@ int dalloc(T** p, size_t count) {
   return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)) == cudaSuccess ? NES_OK : NES_ENOMEM;
 }
 
-bool view_ok(const nes_view& v) {
-  if (v.width == 0 || v.height == 0 || v.width > 16384 || v.height > 16384) return false;
-  if (!(v.focal_px > 0.0f) || !std::isfinite(v.focal_px)) return false;
-  for (float m : v.matrix)
-    if (!std::isfinite(m)) return false;
-  return true;
-}
-
 // Renders views on ctx->stream into the given device outputs.
 int render_batch_locked(nes_ctx* c, const nes_view* views, int n, float* const* rgb, float* const* depth) {
   ViewBatch vb;
@@ -551,6 +543,14 @@ int nes_last_timings(nes_ctx* c, float* raygen_ms, float* march_ms) {
 }  // extern "C"
 
 namespace nes {
+
+bool view_ok(const nes_view& v) {
+  if (v.width == 0 || v.height == 0 || v.width > 16384 || v.height > 16384) return false;
+  if (!(v.focal_px > 0.0f) || !std::isfinite(v.focal_px)) return false;
+  for (float m : v.matrix)
+    if (!std::isfinite(m)) return false;
+  return true;
+}
 
 int fill_view_batch(const nes_view* views, int n, float* const* rgb, float* const* depth, uint64_t max_pixels,
                     ViewBatch* vb, uint64_t* pixels) {

@@ -42,6 +42,11 @@ using Clock = std::chrono::steady_clock;
 namespace {
 
 constexpr int kMaxSlots = 4;
+// The warm-up batch of nes_server_create: one 8x8 view, its RGB24 at byte 0
+// of the slot's RGB24 buffer, Y/U/V planes (linesize 32) at 256/512/768 and
+// uint16 depth at 1024; the buffer holds at least kWarmupBytes.
+constexpr uint32_t kWarmupSide = 8;
+constexpr size_t kWarmupBytes = 1024 + kWarmupSide * kWarmupSide * 2;
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -392,7 +397,9 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
   if (!ctx || !cfg || !out) return NES_EINVAL;
   *out = nullptr;
   if (cfg->max_inflight_batches < 1 || cfg->max_inflight_batches > kMaxSlots) return NES_EINVAL;
-  if (cfg->max_batch_pixels == 0 || cfg->max_batch_pixels > (1u << 27) || cfg->max_pending == 0) return NES_EINVAL;
+  if (cfg->max_batch_pixels < kWarmupSide * kWarmupSide || cfg->max_batch_pixels > (1u << 27) ||
+      cfg->max_pending == 0)
+    return NES_EINVAL;
   if (!(cfg->max_queue_ms >= 0.0f && cfg->max_queue_ms < 1e9f)) return NES_EINVAL;
   if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return NES_ENODEV;
   nes_server* s = new (std::nothrow) nes_server;
@@ -424,7 +431,7 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
     sl.scratch.max_rays = (uint32_t)P;
     if (cudaMalloc(&sl.rgb, P * 3 * sizeof(float)) != cudaSuccess) return fail(NES_ENOMEM);
     if (cudaMalloc(&sl.depth, P * sizeof(float)) != cudaSuccess) return fail(NES_ENOMEM);
-    if (cudaMalloc(&sl.rgb8, P * 3) != cudaSuccess) return fail(NES_ENOMEM);
+    if (cudaMalloc(&sl.rgb8, P * 3 > kWarmupBytes ? P * 3 : kWarmupBytes) != cudaSuccess) return fail(NES_ENOMEM);
     if (cudaMallocHost(&sl.h_counters, kCtrWords * sizeof(uint32_t)) != cudaSuccess) return fail(NES_ENOMEM);
   }
   if (cudaStreamCreateWithFlags(&s->release_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(NES_EIO);
@@ -441,8 +448,8 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
     std::memset(&v, 0, sizeof(v));
     const float M[12] = {1, 0, 0, 0.5f, 0, -1, 0, 0.5f, 0, 0, -1, 0.5f};
     std::memcpy(v.matrix, M, sizeof(M));
-    v.width = v.height = 8;
-    v.focal_px = 4.0f;
+    v.width = v.height = kWarmupSide;
+    v.focal_px = 0.5f * kWarmupSide;
     for (Slot& sl : s->slots) {
       ViewBatch vb;
       uint64_t px = 0;
@@ -452,10 +459,11 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
       if (enqueue_march(vb, ctx->scene, sl.scratch, ctx->cfg.precision, ctx->num_sms, sl.st) != cudaSuccess)
         return fail(NES_EIO);
       const int ls[3] = {32, 32, 32};
-      if (launch_rgb_to_rgb24(sl.rgb, 64 * 3, sl.rgb8, sl.st) != cudaSuccess ||
-          launch_rgb24_to_yuv420p(sl.rgb8, 8, 8, 24, sl.rgb8 + 256, sl.rgb8 + 512, sl.rgb8 + 768, ls, sl.st) !=
-              cudaSuccess ||
-          launch_depth_pack_u16mm(sl.depth, 64, reinterpret_cast<uint16_t*>(sl.rgb8 + 1024), sl.st) != cudaSuccess)
+      const size_t wpx = kWarmupSide * kWarmupSide;
+      if (launch_rgb_to_rgb24(sl.rgb, wpx * 3, sl.rgb8, sl.st) != cudaSuccess ||
+          launch_rgb24_to_yuv420p(sl.rgb8, kWarmupSide, kWarmupSide, 3 * kWarmupSide, sl.rgb8 + 256, sl.rgb8 + 512,
+                                  sl.rgb8 + 768, ls, sl.st) != cudaSuccess ||
+          launch_depth_pack_u16mm(sl.depth, wpx, reinterpret_cast<uint16_t*>(sl.rgb8 + 1024), sl.st) != cudaSuccess)
         return fail(NES_EIO);
       if (cudaStreamSynchronize(sl.st) != cudaSuccess) return fail(NES_EIO);
     }
@@ -492,7 +500,9 @@ int nes_submit(nes_server* s, const nes_request* req, uint64_t* ticket) {
   uint64_t px = 0;
   for (uint32_t v = 0; v < req->nviews; ++v) {
     const nes_view& w = req->views[v];
-    if (w.width == 0 || w.height == 0 || w.width > 16384 || w.height > 16384 || !(w.focal_px > 0.0f)) return NES_EINVAL;
+    // Checked here, not at batch formation, so that a bad view cannot fail
+    // the other requests of its batch.
+    if (!view_ok(w)) return NES_EINVAL;
     if (req->nviews == 2 && (w.width != req->views[0].width || w.height != req->views[0].height)) return NES_EINVAL;
     r.planes[v] = plan_view(w.width, w.height, r.bytes);
     r.bytes += r.planes[v].bytes;
@@ -532,12 +542,18 @@ int nes_wait(nes_server* s, uint64_t ticket, int64_t timeout_ns, nes_result* out
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end()) return NES_EINVAL;
-  auto done = [&] { return s->reqs[ticket].state == ReqState::Done; };
+  // Looked up afresh on each wake-up: another thread may release the ticket
+  // between its completion and this thread's return to the lock.
+  auto done = [&] {
+    it = s->reqs.find(ticket);
+    return it == s->reqs.end() || it->second.state == ReqState::Done;
+  };
   if (timeout_ns < 0)
     s->cv_done.wait(lk, done);
   else if (!s->cv_done.wait_for(lk, std::chrono::nanoseconds(timeout_ns), done))
     return NES_ETIMEDOUT;
-  const Req& r = s->reqs[ticket];
+  if (it == s->reqs.end()) return NES_EINVAL;
+  const Req& r = it->second;
   std::memset(out, 0, sizeof(*out));
   out->ticket = ticket;
   out->status = r.status;

@@ -85,6 +85,25 @@ def test_create_validates_config(nes_lib):
     assert lib.nes_create(ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
 
 
+def test_server_create_validates_config(nes_lib):
+    """nes_server_create checks its configuration before it touches the
+    context or the GPU (the context here is a zeroed stand-in)."""
+    lib = nes_lib.load()
+    ctx = ctypes.create_string_buffer(4096)
+    h = ctypes.c_void_p()
+    for field, value in (("max_batch_pixels", 0), ("max_batch_pixels", 63), ("max_batch_pixels", (1 << 27) + 1),
+                         ("max_inflight_batches", 0), ("max_inflight_batches", 5), ("max_pending", 0),
+                         ("max_queue_ms", -1.0), ("max_queue_ms", float("nan"))):
+        cfg = nes_lib.NesServerConfig()
+        lib.nes_server_config_default(ctypes.byref(cfg))
+        setattr(cfg, field, value)
+        assert lib.nes_server_create(ctx, ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL, (field, value)
+        assert not h.value
+    cfg = nes_lib.NesServerConfig()
+    lib.nes_server_config_default(ctypes.byref(cfg))
+    assert lib.nes_server_create(None, ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
+
+
 def test_create_without_gpu_fails_cleanly(nes_lib):
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():

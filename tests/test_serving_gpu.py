@@ -144,6 +144,32 @@ def test_invalid_requests(nes_lib, server):
         server.submit([left, right])  # stereo eyes must match in size
     with pytest.raises(nes_lib.NesError):
         server.submit([nes_lib.make_view(pose, 0, 64, f)])
+    # Non-finite poses and focal lengths are refused at submission, so they
+    # never reach (and fail) a batch shared with other requests.
+    bad = list(pose)
+    bad[3] = float("nan")
+    for views in ([nes_lib.make_view(bad, 64, 64, f)], [left, nes_lib.make_view(bad, 64, 64, f)],
+                  [nes_lib.make_view(pose, 64, 64, float("inf"))]):
+        with pytest.raises(nes_lib.NesError) as e:
+            server.submit(views)
+        assert e.value.code == nes_lib.NES_EINVAL
+    t = server.submit([left])
+    assert server.wait(t).status == 0
+    server.release(t)
+
+
+def test_smallest_batch_size(nes_lib, rtc):
+    """max_batch_pixels at its minimum (64): the slot buffers still hold the
+    creation-time warm-up batch, and an 8x8 request is served."""
+    pose = nes_lib.shell_poses(8, 1, 1.5, 1.5)[0]
+    with nes_lib.Server(rtc, max_inflight_batches=1, max_batch_pixels=64, hbm_budget_bytes=1 << 26) as srv:
+        t = srv.submit([nes_lib.make_view(pose, 8, 8, nes_lib.focal_from_fov(8, 90.0))])
+        assert t is not None
+        r = srv.wait(t)
+        assert r.status == 0 and r.width == 8 and r.height == 8
+        srv.release(t)
+        with pytest.raises(nes_lib.NesError):
+            srv.submit([nes_lib.make_view(pose, 16, 8, nes_lib.focal_from_fov(16, 90.0))])  # > 64 pixels
 
 
 def test_queue_delay_bound_rejects_late_requests(nes_lib, rtc):
