@@ -23,6 +23,17 @@ struct Reader {
     }
     return false;  // more than 10 bytes
   }
+  // A field key (field number << 3 | wire type).  Like the protobuf
+  // runtime, rejects keys encoded in more than 5 bytes or wider than 32
+  // bits, and field number 0.
+  bool key(uint32_t* field, uint32_t* wire) {
+    const uint8_t* const start = p;
+    uint64_t k;
+    if (!varint(&k) || p - start > 5 || k > 0xFFFFFFFFull || (k >> 3) == 0) return false;
+    *field = (uint32_t)(k >> 3);
+    *wire = (uint32_t)(k & 7);
+    return true;
+  }
   bool bytes(const uint8_t** data, size_t* len) {
     uint64_t l;
     if (!varint(&l)) return false;
@@ -75,10 +86,8 @@ uint8_t* put_varint(uint8_t* o, uint64_t v) {
 bool parse_camera(const uint8_t* p, size_t n, PbCamera* out) {
   Reader r{p, p + n};
   while (r.p < r.end) {
-    uint64_t key;
-    if (!r.varint(&key)) return false;
-    const uint32_t field = (uint32_t)(key >> 3), wire = (uint32_t)(key & 7);
-    if (field == 0) return false;
+    uint32_t field, wire;
+    if (!r.key(&field, &wire)) return false;
     uint64_t v;
     if (field == 2 && wire == 0) {
       if (!r.varint(&v)) return false;
@@ -108,10 +117,8 @@ bool parse_camera(const uint8_t* p, size_t n, PbCamera* out) {
 bool parse_frame_request(const uint8_t* p, size_t n, PbFrameRequest* out) {
   Reader r{p, p + n};
   while (r.p < r.end) {
-    uint64_t key;
-    if (!r.varint(&key)) return false;
-    const uint32_t field = (uint32_t)(key >> 3), wire = (uint32_t)(key & 7);
-    if (field == 0) return false;
+    uint32_t field, wire;
+    if (!r.key(&field, &wire)) return false;
     uint64_t v;
     if (field == 1 && wire == 0) {
       if (!r.varint(&v)) return false;

@@ -81,10 +81,26 @@ def test_unknown_fields_and_unpacked_matrix(nes_lib):
     b"\x0b\x00",                  # wire type 3 (group)
     b"\x00\x01",                  # field number 0
     b"\x12\x03\x62\x01\x00",      # packed matrix length not a multiple of 4
+    b"\x80\x80\x80\x80\x10\x00",  # key 2^32: wider than 32 bits
+    b"\x88\x80\x80\x80\x80\x10\x05",  # key 2^35 + 8: field 1 if truncated to 32 bits
+    b"\x88\x80\x80\x80\x80\x00\x05",  # key of field 1 padded to 6 bytes
+    b"\x08" + b"\x80" * 10 + b"\x00",   # 11-byte varint
 ])
 def test_malformed_requests(nes_lib, bad):
     rc, _ = _parse(nes_lib, bad)
     assert rc == nes_lib.NES_EPROTO
+
+
+@pytest.mark.parametrize("data,index", [
+    (b"\x88\x80\x80\x80\x00\x05", 5),           # key padded to 5 bytes
+    (b"\xf8\xff\xff\xff\x0f\x00\x08\x07", 7),  # field 2^29 - 1 (unknown, skipped)
+    (b"\x08" + b"\xff" * 9 + b"\x02", 2 ** 63 - 1),  # 10th varint byte: bits past 64 dropped
+    (b"\x08" + b"\x80" * 9 + b"\x00", 0),          # 10-byte zero
+])
+def test_edge_encodings_accepted_like_protobuf(nes_lib, data, index):
+    """Outcomes of the official protobuf runtime (7.x, upb) on the same bytes."""
+    rc, out = _parse(nes_lib, data)
+    assert rc == 0 and out.index == index
 
 
 def test_empty_request_parses_to_defaults(nes_lib):
@@ -120,3 +136,54 @@ def test_random_requests_against_protobuf(nes_lib):
         back = RenderedFrame()
         back.ParseFromString(ours)
         assert back == rf
+
+
+def test_mutated_requests_against_protobuf(nes_lib):
+    """Random FrameRequests with bytes overwritten, cut short or inserted:
+    the library accepts exactly what the protobuf runtime accepts and decodes
+    the same values."""
+    pytest.importorskip("google.protobuf")
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from google.protobuf.message import DecodeError
+    from make_golden import nes_proto_classes
+    _, FrameRequest, _ = nes_proto_classes()
+    rng = np.random.default_rng(5)
+    checked = 0
+    for _ in range(4000):
+        req = FrameRequest(index=int(rng.integers(0, 2 ** 63)), is_left=bool(rng.integers(0, 2)))
+        if rng.integers(0, 4):
+            req.camera.is_left = bool(rng.integers(0, 2))
+            req.camera.width = int(rng.integers(0, 5000))
+            req.camera.height = int(rng.integers(0, 5000))
+            req.camera.matrix.extend(rng.uniform(-3, 3, int(rng.integers(0, 13))).astype(np.float32).tolist())
+        data = bytearray(req.SerializeToString())
+        kind = int(rng.integers(0, 3))
+        if kind == 0 and data:
+            for _ in range(int(rng.integers(1, 4))):
+                data[int(rng.integers(0, len(data)))] = int(rng.integers(0, 256))
+        elif kind == 1 and data:
+            data = data[:int(rng.integers(0, len(data)))]
+        else:
+            pos = int(rng.integers(0, len(data) + 1))
+            data = data[:pos] + bytes(rng.integers(0, 256, int(rng.integers(1, 6)), dtype=np.uint8)) + data[pos:]
+        ref = FrameRequest()
+        try:
+            ref.ParseFromString(bytes(data))
+            ok_ref = True
+        except DecodeError:
+            ok_ref = False
+        rc, out = _parse(nes_lib, data)
+        assert (rc == 0) == ok_ref, bytes(data).hex()
+        if not ok_ref:
+            continue
+        checked += 1
+        assert out.index == ref.index and bool(out.is_left) == ref.is_left, bytes(data).hex()
+        assert bool(out.has_camera) == ref.HasField("camera"), bytes(data).hex()
+        if ref.HasField("camera"):
+            m = np.array(list(ref.camera.matrix), np.float32)
+            assert (out.width, out.height, out.matrix_len) == (ref.camera.width, ref.camera.height, len(m))
+            assert bool(out.camera_is_left) == ref.camera.is_left
+            k = min(12, len(m))
+            assert np.array_equal(np.array(out.matrix[:k], np.float32).view(np.uint32), m[:k].view(np.uint32))
+    assert checked > 500
