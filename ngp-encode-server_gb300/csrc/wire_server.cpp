@@ -24,6 +24,7 @@
 #include <atomic>
 #include <cerrno>
 #include <cstring>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -70,7 +71,14 @@ bool recv_all(int fd, uint8_t* p, size_t n, const volatile int* stop) {
   return true;
 }
 
-void serve_connection(nes_ctx* ctx, int fd, const volatile int* stop, std::atomic<uint64_t>* served) {
+// One connection's thread and the flag it sets when it has ended.
+struct Connection {
+  std::thread thread;
+  std::shared_ptr<std::atomic<bool>> ended;
+};
+
+void serve_connection(nes_ctx* ctx, int fd, const volatile int* stop, std::atomic<uint64_t>* served,
+                      std::shared_ptr<std::atomic<bool>> ended) {
   int one = 1;
   setsockopt(fd, IPPROTO_TCP, TCP_NODELAY, &one, sizeof(one));
   std::vector<uint8_t> req, frame;
@@ -92,6 +100,7 @@ void serve_connection(nes_ctx* ctx, int fd, const volatile int* stop, std::atomi
     served->fetch_add(1);
   }
   close(fd);
+  ended->store(true);
 }
 
 }  // namespace
@@ -120,17 +129,35 @@ extern "C" int nes_tcp_serve(nes_ctx* ctx, const char* bind_addr, uint16_t port,
   getsockname(lfd, reinterpret_cast<sockaddr*>(&addr), &alen);
   if (bound_port) *bound_port = ntohs(addr.sin_port);
   std::atomic<uint64_t> served{0};
-  std::vector<std::thread> conns;
+  std::vector<Connection> conns;
   while (!*stop) {
+    // Join the threads of ended connections: clients reconnect after every
+    // failure, and an unjoined thread keeps its stack mapped.
+    for (size_t i = 0; i < conns.size();) {
+      if (conns[i].ended->load()) {
+        conns[i].thread.join();
+        conns[i] = std::move(conns.back());
+        conns.pop_back();
+      } else {
+        ++i;
+      }
+    }
     pollfd pf{lfd, POLLIN, 0};
     const int pr = poll(&pf, 1, 100);
     if (pr <= 0) continue;
     const int fd = accept(lfd, nullptr, nullptr);
     if (fd < 0) continue;
-    conns.emplace_back(serve_connection, ctx, fd, stop, &served);
+    try {
+      conns.reserve(conns.size() + 1);  // the push_back below then cannot throw
+      auto ended = std::make_shared<std::atomic<bool>>(false);
+      std::thread t(serve_connection, ctx, fd, stop, &served, ended);
+      conns.push_back(Connection{std::move(t), std::move(ended)});
+    } catch (...) {  // no thread (or memory) for this connection: refuse it, keep serving
+      close(fd);
+    }
   }
   close(lfd);
-  for (auto& t : conns) t.join();
+  for (Connection& c : conns) c.thread.join();
   if (frames_served) *frames_served = served.load();
   return NES_OK;
 }
