@@ -269,7 +269,8 @@ int nes_trainer_create(nes_ctx *student, const nes_train_config *cfg, nes_traine
 void nes_trainer_destroy(nes_trainer *tr);
 
 /* Target images: nviews views (1..1024) with HWC FP32 RGB and FP32 depth on
- * the device, concatenated view after view (pointers are kept, not copied). */
+ * the device, concatenated view after view (pointers are kept, not copied).
+ * NES_EINVAL for a view that nes_render_views would reject. */
 int nes_trainer_set_targets(nes_trainer *tr, const nes_view *views, int nviews, const float *rgb_dev,
                             const float *depth_dev);
 

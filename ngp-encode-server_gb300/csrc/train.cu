@@ -1478,7 +1478,7 @@ int nes_trainer_set_targets(nes_trainer* t, const nes_view* views, int nviews, c
   uint64_t off = 0;
   for (int i = 0; i < nviews; ++i) {
     const uint64_t px = (uint64_t)views[i].width * views[i].height;
-    if (px == 0 || px > 0x7fffffffull || !(views[i].focal_px > 0.0f)) return NES_EINVAL;
+    if (!view_ok(views[i])) return NES_EINVAL;  // the renderer's own view check
     std::memcpy(hv[i].M, views[i].matrix, sizeof(hv[i].M));
     hv[i].W = (int)views[i].width;
     hv[i].H = (int)views[i].height;
