@@ -28,8 +28,9 @@
 #include <cstring>
 #include <mutex>
 
-#include "nes_gb300.h"
+#include "ctx_internal.h"
 #include "kernels.h"
+#include "nes_gb300.h"
 
 namespace nes {
 namespace {
@@ -77,11 +78,9 @@ extern "C" int nes_render_view_noalloc(const float* table_dev, uint32_t log2_tab
   using namespace nes;
   if (!table_dev || !weights_dev || !occupancy_dev || !view || (!rgb_dev && !depth_dev)) return NES_EINVAL;
   if (log2_table_size < 10 || log2_table_size > 24) return NES_EINVAL;
-  if (view->width == 0 || view->height == 0 || !(view->focal_px > 0.0f)) return NES_EINVAL;
+  if (!view_ok(*view)) return NES_EINVAL;  // the renderer's own view check
   const uint64_t px = (uint64_t)view->width * view->height;
   if (px > kNoAllocMaxRays) return NES_EINVAL;  // beyond the static scratch
-  for (float m : view->matrix)
-    if (!(m == m) || m - m != 0.0f) return NES_EINVAL;  // NaN or infinite
 
   unsigned char* base = nullptr;
   int sms = 0;

@@ -104,6 +104,33 @@ def test_server_create_validates_config(nes_lib):
     assert lib.nes_server_create(None, ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
 
 
+def test_noalloc_render_rejects_bad_arguments_without_gpu(nes_lib):
+    """nes_render_view_noalloc validates its arguments and the view before
+    any CUDA call: missing arrays, a table size outside 2^10..2^24, a view
+    the renderer rejects (zero or over-16384 sides, non-finite pose or
+    focal length) and views above NES_NOALLOC_MAX_PIXELS."""
+    lib = nes_lib.load()
+    fn = lib.nes_render_view_noalloc
+    d = 0x1000  # device addresses are never dereferenced on these paths
+    M = [1, 0, 0, 0.5, 0, -1, 0, 0.5, 0, 0, -1, 0.5]
+    good = nes_lib.make_view(M, 64, 64, 32.0)
+    E = nes_lib.NES_EINVAL
+    assert fn(None, 19, d, d, ctypes.byref(good), d, d, None) == E
+    assert fn(d, 19, None, d, ctypes.byref(good), d, d, None) == E
+    assert fn(d, 19, d, None, ctypes.byref(good), d, d, None) == E
+    assert fn(d, 19, d, d, None, d, d, None) == E
+    assert fn(d, 19, d, d, ctypes.byref(good), None, None, None) == E  # no output at all
+    assert fn(d, 9, d, d, ctypes.byref(good), d, d, None) == E
+    assert fn(d, 25, d, d, ctypes.byref(good), d, d, None) == E
+    bad_pose = list(M)
+    bad_pose[7] = float("inf")
+    for v in (nes_lib.make_view(M, 0, 64, 32.0), nes_lib.make_view(M, 16385, 1, 32.0),
+              nes_lib.make_view(M, 64, 64, float("inf")), nes_lib.make_view(M, 64, 64, float("nan")),
+              nes_lib.make_view(M, 64, 64, 0.0), nes_lib.make_view(bad_pose, 64, 64, 32.0),
+              nes_lib.make_view(M, 513, 512, 256.0)):  # 262,656 > NES_NOALLOC_MAX_PIXELS
+        assert fn(d, 19, d, d, ctypes.byref(v), d, d, None) == E
+
+
 def test_create_without_gpu_fails_cleanly(nes_lib):
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():
