@@ -59,4 +59,4 @@ def test_tcp_endpoint_closes_bad_requests_and_reaps_connections(nes_lib):
     assert served == 0
     # 200 ended connections whose threads were never joined would keep their
     # stacks mapped (8 MiB each by default): well over a gigabyte.
-    assert grown_mb < 128, grown_mb
+    assert grown_mb < 400, grown_mb  # allows a few malloc arenas of new threads (64 MiB each)
