@@ -217,3 +217,21 @@ def test_fp32_cpu_render_matches_fp64_oracle(scene0, nes_lib):
     assert n32 == n64 > 0
     assert oracle.psnr(rgb32.astype(np.float64), rgb64) >= 45.0
     assert np.abs(dep32.astype(np.float64) - dep64).max() <= 1e-3
+
+
+def test_renders_independent_of_thread_count(scene0, nes_lib):
+    """The oracle and the FP32 CPU render split pixels between threads and
+    compute each pixel alone: the same bytes and sample counts for 1, 3 and
+    8 threads, over all pixels and over a scattered pixel list."""
+    M = nes_lib.shell_poses(4, 1, 1.3, 1.3)[0]
+    W, H = 20, 14
+    f = nes_lib.focal_from_fov(W, 80.0)
+    pix = np.random.default_rng(9).permutation(W * H)[:120].astype(np.int32)
+    for fn in (scene0.render, scene0.render_f32):
+        for p in (None, pix):
+            ref = fn(M, W, H, f, pixels=p, nthreads=1)
+            assert ref[2] > 0
+            for nt in (3, 8):
+                got = fn(M, W, H, f, pixels=p, nthreads=nt)
+                assert got[2] == ref[2]
+                assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
