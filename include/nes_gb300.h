@@ -69,7 +69,10 @@ typedef struct nes_config {
 
 /* One view to render: the nes.proto Camera plus a focal length.
  * matrix: 3x4 row-major pose (include/base/camera_manager.h:18-19):
- * columns 0,1,2 = image right, image down, view direction; column 3 = eye. */
+ * columns 0,1,2 = image right, image down, view direction; column 3 = eye.
+ * Every entry point that takes views accepts one when width and height are
+ * 1..16384, focal_px is finite and positive and all 12 matrix entries are
+ * finite, and returns NES_EINVAL otherwise. */
 typedef struct nes_view {
   float matrix[12];
   uint32_t width;
