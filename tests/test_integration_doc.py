@@ -44,6 +44,7 @@ extern float fov_deg;
 extern AVFrame* avframe;
 extern uint16_t* depth_mm;
 extern nes_ctx* nes;
+extern nes_view left_view, right_view;
 extern std::shared_ptr<SwsContextManager> ctxmgr_scene, ctxmgr_depth;
 extern const uint8_t *left_rgb_dev, *right_rgb_dev;
 extern uint8_t *ly, *lu, *lv, *ry, *ru, *rv;
