@@ -485,6 +485,10 @@ void nes_server_destroy(nes_server* s) {
   if (s->sched.joinable()) s->sched.join();
   if (s->comp.joinable()) s->comp.join();
   cudaSetDevice(s->ctx->cfg.device);
+  // A batch launched while the stop was being set may still run (the
+  // completion thread can have left first): its outputs are freed after it.
+  for (Slot& sl : s->slots)
+    if (sl.st) cudaStreamSynchronize(sl.st);
   for (auto& kv : s->reqs)
     if (kv.second.dev) cudaFreeAsync(kv.second.dev, s->release_stream);
   cudaStreamSynchronize(s->release_stream);
