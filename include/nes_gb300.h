@@ -225,8 +225,9 @@ void nes_server_destroy(nes_server *srv);
  * most max_batch_pixels of queued and running pixels. */
 int nes_submit(nes_server *srv, const nes_request *req, uint64_t *ticket);
 
-/* Waits up to timeout_ns (< 0: forever) for the request; NES_ETIMEDOUT when
- * it is not finished yet.  The output pointers stay valid until release. */
+/* Waits up to timeout_ns (< 0 or above 10^15: forever) for the request;
+ * NES_ETIMEDOUT when it is not finished yet.  The output pointers stay valid
+ * until release. */
 int nes_wait(nes_server *srv, uint64_t ticket, int64_t timeout_ns, nes_result *out);
 
 /* Frees a finished request's output slots and its budget share. */

@@ -552,7 +552,9 @@ int nes_wait(nes_server* s, uint64_t ticket, int64_t timeout_ns, nes_result* out
     it = s->reqs.find(ticket);
     return it == s->reqs.end() || it->second.state == ReqState::Done;
   };
-  if (timeout_ns < 0)
+  // Beyond ~11.6 days a timeout counts as none (now + timeout would
+  // overflow the steady clock).
+  if (timeout_ns < 0 || timeout_ns > 1000000000000000ll)
     s->cv_done.wait(lk, done);
   else if (!s->cv_done.wait_for(lk, std::chrono::nanoseconds(timeout_ns), done))
     return NES_ETIMEDOUT;
