@@ -151,6 +151,12 @@ def test_render_server_binary_fails_cleanly_without_gpu(nes_lib):
     assert r.returncode == 1 and "no usable CUDA device" in r.stderr
     r = subprocess.run([nes_build.SERVER_BIN, "--bogus", "1"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 2
+    # Values are checked before the GPU is touched: out-of-range ports and
+    # table sizes, unknown precisions, FOVs outside (0, 180), trailing options.
+    for bad in (["--port", "70000"], ["--port", "12x"], ["--port"], ["--precision", "bf16"],
+                ["--fov", "180"], ["--fov", "abc"], ["--log2-table", "30"], ["--device", "-1"]):
+        r = subprocess.run([nes_build.SERVER_BIN] + bad, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2 and ("bad value" in r.stderr or "needs a value" in r.stderr), bad
 
 
 def test_focal_and_capacity(nes_lib):
