@@ -19,10 +19,12 @@ uint16 mm, all on the device with the scene resident.  L2 is flushed (a
 --impl reference times the plain FP32 CPU render of the path (oracle/, all
 host threads) on bounded random pixel samples of the same requests: the
 reference's renderer is an external project and its swscale/libavcodec
-dependencies are not installed, so the CPU restatement is the CPU arm.  The
-default run's cpu_baseline times the same FP32 CPU render and the FP64
-oracle (the checker) on one pixel sample, with the parity of the
-tensor-core render against the FP64 oracle on those pixels.
+dependencies are not installed, so the CPU restatement is the CPU arm.  That
+arm loads only the oracle's library (poses and focal length are computed in
+Python), and both arms print the same `config`.  The default run's
+cpu_baseline times the same FP32 CPU render and the FP64 oracle (the
+checker) on one pixel sample, with the parity of the tensor-core render
+against the FP64 oracle on those pixels.
 """
 import argparse
 import json
@@ -41,12 +43,20 @@ W, H, FOV, NPOSES, RADIUS = 1920, 1080, 90.0, 100, 1.5
 FLOP_PER_SAMPLE = 18688          # 2 x 9,344 MLP multiply-adds
 GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
 # dram__bytes_read.sum + dram__bytes_write.sum of one full 1920x1080 march
-# launch, from the ncu captures summarised in profiles/march_*_1080p.md.
+# launch (one ncu capture of that launch per kernel, the command
+# `bench.py --steps 1 --warmup 1 --precision <tc|fp32> --no-extras`).
 DRAM_BYTES_PER_LAUNCH = {"fp16": 2815.030e6 + 18.675e6, "fp32": 73.651e6 + 7.437e6}
+DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full 1920x1080 launch"
 # The tensor-core march's binding unit, from the same capture: L1 data-pipe
 # (LSU) wavefronts as a fraction of their peak rate, averaged over SMs.
 L1_WAVEFRONT_FRAC = {"fp16": 0.694}
 WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
+L2_RULE = "flushed (256 MiB write) before every timed GPU step"
+
+
+def bench_config():
+    """The `config` both arms print (identical, so their lines compare)."""
+    return {"workload": WORKLOAD, "l2": L2_RULE, "parallelism": "replicas"}
 
 
 def parse_args():
@@ -160,10 +170,9 @@ def cpu_sample(poses, steps_px, seed, fp32=True):
     subsets; returns (Mrays/s, s, px, threads)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import numpy as np
-    import nes
     import oracle
     scene = oracle.Scene(0, 19)
-    f = nes.focal_from_fov(W, FOV)
+    f = oracle.focal_from_fov(W, FOV)
     rng = np.random.default_rng(seed)
     threads = os.cpu_count() or 1
     total_px, total_s = 0, 0.0
@@ -181,6 +190,8 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    # Poses are pure Python (nes.shell_poses loads no library); the focal
+    # length comes from the oracle: this arm maps only the oracle's library.
     import nes
     poses = nes.shell_poses(0, NPOSES, RADIUS, RADIUS)
     per_step = max(2048, (W * H) // 256)
@@ -190,11 +201,11 @@ def run_reference(args):
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and poses)",
-            "config": {"workload": WORKLOAD, "sample": "%d random pixels per step" % per_step,
-                       "l2": "n/a (CPU)"},
+            "config": bench_config(),
             "cpu_baseline": {"value": round(mrays, 6), "unit": "Mrays/s", "cores": threads, "kind": "port",
                              "sample": "plain FP32 CPU render (oracle/, pthreads) of %d random pixels of a "
-                                       "1920x1080 request per step, %d steps" % (per_step, args.steps)},
+                                       "1920x1080 request per step (misses included in proportion), %d steps; "
+                                       "Mrays/s = sampled pixels / CPU time" % (per_step, args.steps)},
             "e2e": {"value": round(mrays, 6), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -314,8 +325,9 @@ def run_ours(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(head["ms_per_step"], 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": kind, "data": "synthetic (seeded scene and poses)",
-        "config": {"workload": WORKLOAD, "precision": "FP16 tcgen05" if kind == "fp16" else "FP32 CUDA cores",
-                   "l2": "flushed (256 MiB write) before every timed step", "parallelism": "replicas"},
+        "config": bench_config(),
+        "precision": "FP16 table + FP16 MLP on tcgen05, FP32 accumulate and compositing" if kind == "fp16"
+                     else "FP32 CUDA cores",
         "e2e": {"value": round(head["e2e"]["mrays"], 3), "unit": "Mrays/s",
                 "h2d_bytes_per_step": head["e2e"]["h2d"], "d2h_bytes_per_step": head["e2e"]["d2h"],
                 "p50_ms": round(head["e2e"]["p50_ms"], 3), "p99_ms": round(head["e2e"]["p99_ms"], 3)},
@@ -327,7 +339,7 @@ def run_ours(args):
                                      "records of levels 0-6 (70 MB) stay in L2, those of levels 7-9 (1.23 GB) "
                                      "come from HBM; the 512 B/sample of gathers are served mostly by L1/L2",
                      "limiter": "hash-table gathers: L1 data pipe at 69-73% of its wavefront rate, ALU 40%, "
-                                "tensor pipe 11% (ncu, profiles/march_tc_1080p.md)",
+                                "tensor pipe 11% (ncu capture of one 1920x1080 march launch)",
                      "l1_wavefront_frac": L1_WAVEFRONT_FRAC.get(kind),
                      "kernel": "march", "peak_source": src + " bf16 sustained",
                      "march_ms": round(head["march_ms"], 3), "raygen_ms": round(head["raygen_ms"], 4),

@@ -14,7 +14,7 @@
  *  (ii) The frame glue.  RenderedFrame::convert_frame converts the RGB24 scene
  *       and GRAY8 depth planes to YUV420P with libswscale
  *       (include/base/video/rendered_frame.h:24-33,
- *       src/base/video/type_managers.cc:241-251).  nes_rgb24_to_yuv420p() and
+ *       src/base/video/type_managers.cc:143-153).  nes_rgb24_to_yuv420p() and
  *       nes_gray8_to_yuv420p() write the same YUV420P plane layout that
  *       AVCodecContextManager::send_frame consumes (src/encode.cpp:136-137,
  *       164-165); nes_depth_pack_u16mm() packs FP32 depth to uint16 mm.

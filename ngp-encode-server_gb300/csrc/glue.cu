@@ -2,7 +2,7 @@
 // quantisation.  They replace RenderedFrame::convert_frame, which runs
 // libswscale on the CPU once per eye and frame
 // (include/base/video/rendered_frame.h:24-33,
-// src/base/video/type_managers.cc:241-251), writing the YUV420P plane layout
+// src/base/video/type_managers.cc:143-153), writing the YUV420P plane layout
 // that AVCodecContextManager::send_frame consumes (src/encode.cpp:136-137).
 //
 // Conversion: ITU-R BT.601 studio range in fixed point (coefficients in

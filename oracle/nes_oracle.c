@@ -24,7 +24,7 @@
  *
  *  - RenderedFrame::convert_frame (include/base/video/rendered_frame.h:24-33),
  *    i.e. libswscale RGB24->YUV420P and GRAY8->YUV420P at the frame's own
- *    size (src/base/video/type_managers.cc:241-251).  libswscale is not
+ *    size (src/base/video/type_managers.cc:143-153).  libswscale is not
  *    installed in this container nor on the GPU host, so this is the repo's
  *    own integer restatement of ITU-R BT.601 studio-range conversion with
  *    2x2 chroma averaging.  SWSCALE PARITY UNPINNED; the restatement is pinned
@@ -33,7 +33,7 @@
  *  - Depth packing FP32 scene units -> uint16 millimetres (new in the
  *    GB300 build; the reference ships GRAY8 depth, src/server.cpp:193-194).
  *
- * Build: oracle/build_oracle.sh (gcc -O2 -ffp-contract=off, no fast-math:
+ * Build: oracle/build_oracle.py (gcc -O2 -ffp-contract=off, no fast-math:
  * the FP32 ray set-up must round exactly like the CUDA kernels' *_rn ops).
  */
 #include <math.h>

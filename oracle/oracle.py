@@ -7,6 +7,7 @@ output (the reference ships no renderer, no swscale call that can run here,
 and no test vectors); see the header of nes_oracle.c for what pins it.
 """
 import ctypes
+import math
 import os
 
 import numpy as np
@@ -194,6 +195,14 @@ class Scene:
             n = self.param(k).size
             self.set_param(k, blob[off:off + n])
             off += n
+
+
+def focal_from_fov(width, fov_deg):
+    """Focal length in pixels for a horizontal FOV: (W/2) / tan(FOV/2) in
+    double, rounded once to float32 (the camera convention of the scene
+    specification, the same rounding the CUDA library applies)."""
+    half = 0.5 * float(np.float32(fov_deg)) * 3.14159265358979323846 / 180.0
+    return float(np.float32(0.5 * float(width) / math.tan(half)))
 
 
 def ray_setup(matrix, W, H, focal, px, py):

@@ -90,3 +90,29 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "0"], capture_output=True, text=True, timeout=300, cwd=REPO, env=env)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_reference_arm_maps_no_product_library():
+    """The reference arm times the CPU restatement only: the process maps the
+    oracle's library and never the CUDA library, and its `config` is the
+    one the GPU arm prints."""
+    import json
+    import subprocess
+    code = ("import sys, json, argparse; sys.argv=['bench.py']; sys.path.insert(0, %r); import bench; "
+            "a = argparse.Namespace(gpus=1, steps=1, warmup=0); bench.run_reference(a); "
+            "maps = open('/proc/self/maps').read(); "
+            "print(json.dumps({'nes': 'libnes_gb300' in maps, 'oracle': 'liboracle' in maps, "
+            "'config': bench.bench_config()}))" % REPO)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    line, probe = lines[0], lines[-1]
+    assert probe["oracle"] and not probe["nes"]
+    assert line["config"] == probe["config"]
+
+
+def test_oracle_focal_matches_library(nes_lib):
+    import oracle
+    for w in (1, 33, 400, 800, 1280, 1920, 4096):
+        for fov in (45.5, 60.0, 90.0, 100.0, 120.0):
+            assert oracle.focal_from_fov(w, fov) == nes_lib.focal_from_fov(w, fov)
