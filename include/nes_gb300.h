@@ -153,7 +153,8 @@ int nes_render_yuv(nes_ctx *ctx, const nes_view *view, uint8_t *y_host, uint8_t 
  * NES_NOALLOC_MAX_PIXELS pixels return NES_EINVAL.  All calls on a device
  * share that array: calls whose GPU work overlaps race.  The first call on
  * a device looks up the array's address (make it before any stream capture
- * on that device). */
+ * on that device) and keeps it for the life of the process, so a
+ * cudaDeviceReset of that device after the first call is not supported. */
 int nes_render_view_noalloc(const float *table_dev, uint32_t log2_table_size, const float *weights_dev,
                             const uint32_t *occupancy_dev, const nes_view *view, float *rgb_dev,
                             float *depth_dev, void *stream);
@@ -424,6 +425,17 @@ int nes_rebuild_occupancy(nes_ctx *ctx, float threshold);
 
 /* Number of field evaluations (samples) of the last render call. */
 int nes_last_sample_count(nes_ctx *ctx, uint64_t *samples);
+
+/* Self-test of the device-side bounded waits (every spin in the tensor-core
+ * kernels gives up after a poll limit and reports NES_ETIMEDOUT instead of
+ * hanging; neserver's analogue is the 1 s LockTimeout of its frame queue,
+ * src/base/video/frame_queue.cc:14-22).  One CTA allocates tensor memory,
+ * waits with the kernels' bounded mbarrier wait for at most poll_limit polls
+ * (1..2^24) on a barrier nothing arrives at (arrive = 0) or one it completed
+ * itself (arrive = 1), and leaves through the kernels' uniform exit.
+ * Returns NES_ETIMEDOUT when the wait ran out, NES_OK when it completed; the
+ * context stays usable either way.  Blocks until done. */
+int nes_selftest_bounded_wait(nes_ctx *ctx, uint32_t poll_limit, int arrive);
 
 /* Per-kernel timing with CUDA events recorded on the stream the kernels
  * run on (the reference's ScopedTimer averages, src/server.cpp:172-190,

@@ -93,6 +93,12 @@ cudaError_t launch_yuv420p_batch(bool gray, const FrameSet& fs, int nframes, int
                                  const int ls[3], cudaStream_t stream);
 cudaError_t launch_depth_pack_u16mm_batch(const DepthSet& ds, int nframes, size_t n, cudaStream_t stream);
 
+// Self-test of the bounded device waits: one CTA waits (at most poll_limit
+// polls, 1..2^24) on an mbarrier nothing arrives at (arrive = 0) or that it
+// completed itself (arrive = 1), and sets counters[kCtrError] when the wait
+// ran out.
+cudaError_t launch_bounded_wait_probe(uint32_t poll_limit, int arrive, uint32_t* counters, cudaStream_t stream);
+
 // FP32 -> FP16 table conversion (level-major, same indexing).
 cudaError_t launch_table_to_fp16(const float2* src, __half2* dst, size_t n, cudaStream_t stream);
 

@@ -518,6 +518,22 @@ int nes_last_sample_count(nes_ctx* c, uint64_t* samples) {
   return rc;
 }
 
+int nes_selftest_bounded_wait(nes_ctx* c, uint32_t poll_limit, int arrive) {
+  if (!c || poll_limit == 0 || poll_limit > (1u << 24)) return NES_EINVAL;
+  std::lock_guard<std::mutex> lock(c->mu);
+  NES_CUDA(cudaSetDevice(c->cfg.device));
+  // Settle the previous render's sample count before the counters are reused.
+  NES_CUDA(cudaStreamSynchronize(c->stream));
+  const int prev = collect_status(c);
+  if (prev != NES_OK) return prev;
+  NES_CUDA(cudaMemsetAsync(c->scratch.counters, 0, kCtrWords * sizeof(uint32_t), c->stream));
+  NES_CUDA(launch_bounded_wait_probe(poll_limit, arrive ? 1 : 0, c->scratch.counters, c->stream));
+  uint32_t err = 0;
+  NES_CUDA(cudaMemcpyAsync(&err, c->scratch.counters + kCtrError, sizeof(err), cudaMemcpyDeviceToHost, c->stream));
+  NES_CUDA(cudaStreamSynchronize(c->stream));
+  return err ? NES_ETIMEDOUT : NES_OK;
+}
+
 int nes_set_profiling(nes_ctx* c, int enable) {
   if (!c) return NES_EINVAL;
   std::lock_guard<std::mutex> lock(c->mu);

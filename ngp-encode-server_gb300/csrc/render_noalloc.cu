@@ -22,7 +22,10 @@
 //    host threads, without ordering between them) race on the array.
 //  - the first call on a device (per process) looks up the array's device
 //    address with cudaGetSymbolAddress, with that device current; make that
-//    first call before any stream capture on that device.
+//    first call before any stream capture on that device.  The address is
+//    kept for the life of the process: a cudaDeviceReset of the device after
+//    that first call (which unloads the module and its array) is not
+//    supported.
 #include <cuda_runtime.h>
 
 #include <cstring>
