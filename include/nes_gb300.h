@@ -135,6 +135,20 @@ int nes_render_views(nes_ctx *ctx, const nes_view *views, int nviews, float *con
 int nes_render_yuv(nes_ctx *ctx, const nes_view *view, uint8_t *y_host, uint8_t *u_host,
                    uint8_t *v_host, const int linesize[3], uint16_t *depth_mm_host);
 
+/* Pose -> YUV end to end for nviews views of one size rendered as one batch
+ * (e.g. the left and right eye of a stereo request, which neserver asks the
+ * renderer for one eye at a time, src/server.cpp:144-161): one march over all
+ * views' rays, one frame-output launch for all views, then the planes of
+ * view i are copied to y_host[i], u_host[i], v_host[i] (all with
+ * linesize[3]) and, where depth_mm_host is not NULL and depth_mm_host[i] is
+ * not NULL, its W*H uint16 depth to depth_mm_host[i].  Each view's bytes are
+ * those nes_render_yuv gives for it alone.  Blocks until the host buffers are
+ * filled.  NES_EINVAL for views of different sizes or beyond the context's
+ * max_pixels. */
+int nes_render_yuv_views(nes_ctx *ctx, const nes_view *views, int nviews, uint8_t *const *y_host,
+                         uint8_t *const *u_host, uint8_t *const *v_host, const int linesize[3],
+                         uint16_t *const *depth_mm_host);
+
 /* Largest view (width * height) nes_render_view_noalloc accepts. */
 #define NES_NOALLOC_MAX_PIXELS (1u << 18) /* 262,144 pixels, e.g. 512 x 512 */
 
@@ -166,9 +180,13 @@ int nes_render_view_noalloc(const float *table_dev, uint32_t log2_table_size, co
  * frame_queue.cc:11-39, frame_map.cc:12-53).  Requests are admitted against a
  * device-memory budget; a scheduler thread flattens the views of all waiting
  * requests (mono or stereo, any resolution) into one ray queue per batch and
- * keeps up to max_inflight_batches batches on the GPU, each captured as a
- * CUDA graph reused per batch shape.  Outputs (YUV420P planes + uint16 depth)
- * stay in device-resident slots until the caller releases them. */
+ * keeps up to max_inflight_batches batches on the GPU.  Each batch slot owns
+ * one CUDA graph, captured and instantiated once at creation, whose kernels
+ * read the batch (views, poses, output planes) from a device-side descriptor:
+ * every batch of any shape replays it.  Outputs (YUV420P planes + uint16
+ * depth) are carved at admission out of a device output arena allocated once
+ * at creation (the budget minus the fixed per-slot buffers) and stay there
+ * until the caller releases them: nothing is allocated on the request path. */
 
 typedef struct nes_server nes_server;
 
@@ -205,7 +223,8 @@ typedef struct nes_result {
 typedef struct nes_server_stats {
   uint64_t submitted, rejected, completed, batches;
   uint64_t pixels, samples;
-  uint64_t graph_instantiations, graph_updates;
+  uint64_t graph_instantiations; /* one per slot, at creation (0 with use_graphs = 0) */
+  uint64_t graph_updates;        /* graph updates after creation: always 0 */
   uint64_t budget_used_bytes;
 } nes_server_stats;
 
@@ -214,6 +233,10 @@ typedef struct nes_server_stats {
 void nes_server_config_default(nes_server_config *cfg);
 
 int nes_server_create(nes_ctx *ctx, const nes_server_config *cfg, nes_server **out);
+/* Stops the scheduler, waits for the batches on the GPU and frees the
+ * server.  Requests still pending (never batched) finish with NES_EIO.
+ * nes_submit, nes_wait and nes_release must not run concurrently with it or
+ * after it. */
 void nes_server_destroy(nes_server *srv);
 
 /* Admits a request.  NES_EAGAIN when the budget or the pending queue is

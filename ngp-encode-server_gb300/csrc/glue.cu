@@ -333,6 +333,48 @@ __global__ void rgb_to_rgb24_kernel(const float* __restrict__ rgb, size_t n, uin
   for (size_t i = done + i0; i < n; i += stride) out[i] = unit_q(rgb[i]);
 }
 
+// Fused frame output: one thread per 2x2 pixel block of a view of the
+// batch.  Each pixel's FP32 colour is quantised to RGB24 (unit_q), its luma
+// written, the block's chroma computed from the quantised 2x2 sum (edge
+// pixels replicated for odd sizes, as rgb24_to_yuv420p does) and its depth
+// packed to uint16 mm: byte for byte the three-kernel sequence, without the
+// RGB24 intermediate in memory.
+template <class Src>
+__global__ void __launch_bounds__(kGlueThreads) frame_out_kernel(const __grid_constant__ Src src) {
+  const FrameBatch& fb = src.get();
+  const uint32_t total = fb.total_blocks;
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
+    int vi = 0;
+    while (vi + 1 < fb.n && b >= fb.f[vi + 1].first_block) ++vi;
+    const FrameOut& F = fb.f[vi];
+    const uint32_t local = b - F.first_block;
+    const uint32_t cw = (uint32_t)(F.w + 1) >> 1;
+    const int cx = (int)(local % cw), cy = (int)(local / cw);
+    int sr = 0, sg = 0, sb = 0;
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy) {
+      const int yy = 2 * cy + dy;
+      const size_t row = (size_t)min(yy, F.h - 1) * (size_t)F.w;
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const int xx = 2 * cx + dx;
+        const size_t p = row + (size_t)min(xx, F.w - 1);
+        const int r = unit_q(__ldg(F.rgb + 3 * p)), g = unit_q(__ldg(F.rgb + 3 * p + 1)),
+                  bl = unit_q(__ldg(F.rgb + 3 * p + 2));
+        sr += r;
+        sg += g;
+        sb += bl;
+        if (yy < F.h && xx < F.w) {
+          F.y[(size_t)yy * F.ls0 + xx] = luma(r, g, bl);
+          if (F.depth_mm) F.depth_mm[p] = pack_mm(__ldg(F.depth + p));
+        }
+      }
+    }
+    F.u[(size_t)cy * F.ls1 + cx] = clamp8((kUR * sr + kUG * sg + kUB * sb + (128 << 18) + (1 << 17)) >> 18);
+    F.v[(size_t)cy * F.ls2 + cx] = clamp8((kVR * sr + kVG * sg + kVB * sb + (128 << 18) + (1 << 17)) >> 18);
+  }
+}
+
 unsigned grid_for(size_t n) {
   size_t b = (n + 4 * kGlueThreads - 1) / (4 * kGlueThreads);
   if (b > 152 * 8) b = 152 * 8;  // grid-stride beyond 8 resident blocks per SM
@@ -418,6 +460,27 @@ cudaError_t launch_depth_pack_u16mm_batch(const DepthSet& ds, int nframes, size_
   unsigned gx = grid_for(n * (size_t)nframes) / (unsigned)nframes;
   dim3 grid(gx ? gx : 1, nframes);
   depth_pack_u16mm_batch_kernel<<<grid, kGlueThreads, 0, stream>>>(ds, n, vec);
+  return cudaGetLastError();
+}
+
+void frame_batch_index(FrameBatch* fb) {
+  uint32_t blocks = 0;
+  for (int i = 0; i < fb->n; ++i) {
+    fb->f[i].first_block = blocks;
+    blocks += (uint32_t)((fb->f[i].w + 1) / 2) * (uint32_t)((fb->f[i].h + 1) / 2);
+  }
+  fb->total_blocks = blocks;
+}
+
+cudaError_t launch_frame_out(const FrameBatch& fb, cudaStream_t stream) {
+  if (fb.total_blocks == 0) return cudaSuccess;
+  frame_out_kernel<<<(fb.total_blocks + kGlueThreads - 1) / kGlueThreads, kGlueThreads, 0, stream>>>(
+      InParam<FrameBatch>{fb});
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frame_out(const FrameBatch* fb_dev, int num_sms, cudaStream_t stream) {
+  frame_out_kernel<<<(unsigned)num_sms * 8u, kGlueThreads, 0, stream>>>(InMemory<FrameBatch>{fb_dev});
   return cudaGetLastError();
 }
 

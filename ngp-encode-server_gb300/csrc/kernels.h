@@ -41,16 +41,24 @@ constexpr int kCtrWords = 8;
 // Ray generation + unit-cube clip + warp-ballot compaction of hits; writes
 // zero colour/depth for pixels whose ray misses.  counters must be zeroed.
 cudaError_t launch_raygen(const ViewBatch& views, const DevScratch& s, cudaStream_t stream);
+// The same with the batch descriptor read from device memory at run time (a
+// fixed grid sized for max_pixels, so a captured graph serves any batch).
+cudaError_t launch_raygen(const ViewBatch* views_dev, uint32_t max_pixels, int num_sms, const DevScratch& s,
+                          cudaStream_t stream);
 
 // Plain FP32 march: persistent CTAs pull compacted rays, evaluate the FP32
 // table + FP32 MLP on CUDA cores and composite.
 cudaError_t launch_march_fp32(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
                               int num_sms, cudaStream_t stream);
+cudaError_t launch_march_fp32(const ViewBatch* views_dev, const DevScene& scene, const DevScratch& s, int num_sms,
+                              cudaStream_t stream);
 
 // FP16 tensor-core march (tcgen05 MLP).  Needs scene.table16 and
 // scene.tc_weights (the FP16 operand image from launch_pack_tc_weights).
 cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s,
                             int num_sms, cudaStream_t stream);
+cudaError_t launch_march_tc(const ViewBatch* views_dev, const DevScene& scene, const DevScratch& s, int num_sms,
+                            cudaStream_t stream);
 
 // Bytes of the per-cell corner records and their construction from the FP16
 // table (tensor-core path).
@@ -75,6 +83,16 @@ cudaError_t launch_depth_pack_u16mm(const float* d, size_t n, uint16_t* out, cud
 cudaError_t launch_depth_to_gray8(const float* d, size_t n, float dmax, uint8_t* out,
                                   cudaStream_t stream);
 cudaError_t launch_rgb_to_rgb24(const float* rgb, size_t n, uint8_t* out, cudaStream_t stream);
+
+// Fused frame output of a rendered batch: per view, FP32 RGB -> RGB24
+// quantisation -> YUV420P and FP32 depth -> uint16 mm in one pass, the
+// same bytes as launch_rgb_to_rgb24 + launch_rgb24_to_yuv420p +
+// launch_depth_pack_u16mm.  Descriptor by value (grid sized to the batch) or
+// in device memory (fixed grid of num_sms x 8 blocks, grid-stride).
+cudaError_t launch_frame_out(const FrameBatch& fb, cudaStream_t stream);
+cudaError_t launch_frame_out(const FrameBatch* fb_dev, int num_sms, cudaStream_t stream);
+// Fills fb->f[i].first_block and fb->total_blocks from the views' sizes.
+void frame_batch_index(FrameBatch* fb);
 
 // Batched frame glue: up to kMaxBatchFrames frames of one geometry per
 // launch, per-frame device pointers passed by value.

@@ -266,8 +266,10 @@ __device__ __forceinline__ void skip_empty(const DevScene& sc, Slot& q) {
   while (q.ei < q.n && !occupied(sc.occ, sample_pos(q.o, q.d, fmaf((float)q.ei + 0.5f, kDt, q.ts)))) ++q.ei;
 }
 
+template <class Src>
 __global__ void __launch_bounds__(kTcThreads, 1)
-march_tc_kernel(const ViewBatch vb, const DevScene sc, const DevScratch s) {
+march_tc_kernel(const __grid_constant__ Src src, const DevScene sc, const DevScratch s) {
+  const ViewBatch& vb = src.get();
   extern __shared__ __align__(128) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + kSmemAlign - 1) &
                                              ~uintptr_t(kSmemAlign - 1));
@@ -609,30 +611,46 @@ cudaError_t launch_pack_tc_weights(const float* w32, uint8_t* out, cudaStream_t 
   return cudaGetLastError();
 }
 
-cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
-                            cudaStream_t stream) {
+namespace {
+
+template <class Src>
+cudaError_t launch_march_tc_src(const Src& src, const DevScene& scene, const DevScratch& s, int num_sms,
+                                cudaStream_t stream) {
   if (!scene.table16 || !scene.rec16 || !scene.tc_weights) return cudaErrorInvalidValue;
   if (s.max_rays > kIdMask) return cudaErrorInvalidValue;  // ray ids share a word with the flags
   static bool attr_set = false;  // idempotent; a race only repeats the calls
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRequest);
+    cudaError_t e =
+        cudaFuncSetAttribute(march_tc_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRequest);
     if (e != cudaSuccess) return e;
     // 14 % of 228 KiB selects the 32 KiB configuration, which holds the
     // request: the rest of the SM's 256 KiB stays L1 for the table gathers.
-    e = cudaFuncSetAttribute(march_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 14);
+    e = cudaFuncSetAttribute(march_tc_kernel<Src>, cudaFuncAttributePreferredSharedMemoryCarveout, 14);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   // One CTA per SM is what makes the 512-column TMEM allocation safe: two
   // 1024-thread CTAs fit on an SM only at <= 32 registers per thread.
   cudaFuncAttributes fa;
-  cudaError_t e = cudaFuncGetAttributes(&fa, march_tc_kernel);
+  cudaError_t e = cudaFuncGetAttributes(&fa, march_tc_kernel<Src>);
   if (e != cudaSuccess) return e;
   // The setmaxnreg split hands out exactly 1024 x kLaunchRegs registers: a
   // build with a smaller launch allocation would stall the encoders' increase.
   if (fa.numRegs != (int)kLaunchRegs) return cudaErrorInvalidConfiguration;
-  march_tc_kernel<<<num_sms, kTcThreads, kSmemRequest, stream>>>(views, scene, s);
+  march_tc_kernel<Src><<<num_sms, kTcThreads, kSmemRequest, stream>>>(src, scene, s);
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_march_tc(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
+                            cudaStream_t stream) {
+  return launch_march_tc_src(InParam<ViewBatch>{views}, scene, s, num_sms, stream);
+}
+
+cudaError_t launch_march_tc(const ViewBatch* views_dev, const DevScene& scene, const DevScratch& s, int num_sms,
+                            cudaStream_t stream) {
+  return launch_march_tc_src(InMemory<ViewBatch>{views_dev}, scene, s, num_sms, stream);
 }
 
 }  // namespace nes

@@ -274,34 +274,73 @@ int nes_render_views(nes_ctx* c, const nes_view* views, int nviews, float* const
   return on_ctx_stream(c, stream, [&] { return render_batch_locked(c, views, nviews, rgb_dev, depth_dev); });
 }
 
-int nes_render_yuv(nes_ctx* c, const nes_view* view, uint8_t* y_host, uint8_t* u_host, uint8_t* v_host,
-                   const int linesize[3], uint16_t* depth_mm_host) {
-  if (!c || !view || !y_host || !u_host || !v_host || !linesize) return NES_EINVAL;
-  const int w = (int)view->width, h = (int)view->height;
+int nes_render_yuv_views(nes_ctx* c, const nes_view* views, int nviews, uint8_t* const* y_host,
+                         uint8_t* const* u_host, uint8_t* const* v_host, const int linesize[3],
+                         uint16_t* const* depth_mm_host) {
+  if (!c || !views || !y_host || !u_host || !v_host || !linesize || nviews < 1 || nviews > kMaxViews)
+    return NES_EINVAL;
+  const int w = (int)views[0].width, h = (int)views[0].height;
+  for (int i = 0; i < nviews; ++i) {
+    if ((int)views[i].width != w || (int)views[i].height != h) return NES_EINVAL;
+    if (!y_host[i] || !u_host[i] || !v_host[i]) return NES_EINVAL;
+  }
   if (!planes_ok(w, h, linesize)) return NES_EINVAL;
   const int ch = (h + 1) / 2;
   const size_t ysz = (size_t)linesize[0] * h, usz = (size_t)linesize[1] * ch, vsz = (size_t)linesize[2] * ch;
-  if (ysz + usz + vsz > c->yuv_capacity) return NES_EINVAL;
   const size_t px = (size_t)w * h;
+  if ((ysz + usz + vsz) * (size_t)nviews > c->yuv_capacity) return NES_EINVAL;
+  if (px * (size_t)nviews > c->cfg.max_pixels) return NES_EINVAL;
   std::lock_guard<std::mutex> lock(c->mu);
   NES_CUDA(cudaSetDevice(c->cfg.device));
-  float* rgb[1] = {c->d_rgb};
-  float* dep[1] = {c->d_depth};
-  int rc = render_batch_locked(c, view, 1, rgb, dep);
+  float* rgb[kMaxViews];
+  float* dep[kMaxViews];
+  for (int i = 0; i < nviews; ++i) {
+    rgb[i] = c->d_rgb + 3 * px * (size_t)i;
+    dep[i] = c->d_depth + px * (size_t)i;
+  }
+  int rc = render_batch_locked(c, views, nviews, rgb, dep);
   if (rc != NES_OK) return rc;
-  uint8_t* dy = c->d_yuv;
-  uint8_t* du = dy + ysz;
-  uint8_t* dv = du + usz;
-  NES_CUDA(launch_rgb_to_rgb24(c->d_rgb, px * 3, c->d_rgb8, c->stream));
-  NES_CUDA(launch_rgb24_to_yuv420p(c->d_rgb8, w, h, w * 3, dy, du, dv, linesize, c->stream));
-  if (depth_mm_host) NES_CUDA(launch_depth_pack_u16mm(c->d_depth, px, c->d_depth16, c->stream));
-  NES_CUDA(cudaMemcpyAsync(y_host, dy, ysz, cudaMemcpyDeviceToHost, c->stream));
-  NES_CUDA(cudaMemcpyAsync(u_host, du, usz, cudaMemcpyDeviceToHost, c->stream));
-  NES_CUDA(cudaMemcpyAsync(v_host, dv, vsz, cudaMemcpyDeviceToHost, c->stream));
-  if (depth_mm_host)
-    NES_CUDA(cudaMemcpyAsync(depth_mm_host, c->d_depth16, px * sizeof(uint16_t), cudaMemcpyDeviceToHost, c->stream));
+  // RGB24 quantisation, YUV420P and depth packing of every view in one launch.
+  FrameBatch fb;
+  std::memset(&fb, 0, sizeof(fb));
+  fb.n = nviews;
+  for (int i = 0; i < nviews; ++i) {
+    FrameOut& F = fb.f[i];
+    F.rgb = rgb[i];
+    F.depth = dep[i];
+    F.y = c->d_yuv + (ysz + usz + vsz) * (size_t)i;
+    F.u = F.y + ysz;
+    F.v = F.u + usz;
+    F.depth_mm = depth_mm_host && depth_mm_host[i] ? c->d_depth16 + px * (size_t)i : nullptr;
+    F.w = w;
+    F.h = h;
+    F.ls0 = linesize[0];
+    F.ls1 = linesize[1];
+    F.ls2 = linesize[2];
+  }
+  frame_batch_index(&fb);
+  NES_CUDA(launch_frame_out(fb, c->stream));
+  for (int i = 0; i < nviews; ++i) {
+    const FrameOut& F = fb.f[i];
+    NES_CUDA(cudaMemcpyAsync(y_host[i], F.y, ysz, cudaMemcpyDeviceToHost, c->stream));
+    NES_CUDA(cudaMemcpyAsync(u_host[i], F.u, usz, cudaMemcpyDeviceToHost, c->stream));
+    NES_CUDA(cudaMemcpyAsync(v_host[i], F.v, vsz, cudaMemcpyDeviceToHost, c->stream));
+    if (F.depth_mm)
+      NES_CUDA(cudaMemcpyAsync(depth_mm_host[i], F.depth_mm, px * sizeof(uint16_t), cudaMemcpyDeviceToHost,
+                               c->stream));
+  }
   NES_CUDA(cudaStreamSynchronize(c->stream));
   return collect_status(c);
+}
+
+int nes_render_yuv(nes_ctx* c, const nes_view* view, uint8_t* y_host, uint8_t* u_host, uint8_t* v_host,
+                   const int linesize[3], uint16_t* depth_mm_host) {
+  if (!c || !view) return NES_EINVAL;
+  uint8_t* y[1] = {y_host};
+  uint8_t* u[1] = {u_host};
+  uint8_t* v[1] = {v_host};
+  uint16_t* d[1] = {depth_mm_host};
+  return nes_render_yuv_views(c, view, 1, y, u, v, linesize, d);
 }
 
 int nes_rgb24_to_yuv420p(const uint8_t* rgb_dev, int width, int height, int rgb_linesize, uint8_t* y_dev,

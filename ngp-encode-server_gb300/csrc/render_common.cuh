@@ -38,6 +38,39 @@ struct ViewBatch {
   DevView v[kMaxViews];
 };
 
+// Per-view frame output of a batch: the FP32 render (HWC RGB, depth) in, the
+// YUV420P planes (caller linesizes) and uint16 millimetre depth out.
+struct FrameOut {
+  const float* rgb;
+  const float* depth;
+  uint8_t *y, *u, *v;
+  uint16_t* depth_mm;  // may be null
+  int w, h;
+  int ls0, ls1, ls2;
+  uint32_t first_block;  // first 2x2 pixel block of this view in the batch
+};
+
+struct FrameBatch {
+  int n;
+  uint32_t total_blocks;  // sum over views of ceil(w/2) * ceil(h/2)
+  FrameOut f[kMaxViews];
+};
+
+// Where a kernel finds its batch descriptor: in its own parameters (one
+// launch per batch), or in device memory, so that one instantiated CUDA
+// graph serves every batch -- the host rewrites the descriptor before each
+// replay and the graph's nodes never change.
+template <class T>
+struct InParam {
+  T d;
+  __device__ __forceinline__ const T& get() const { return d; }
+};
+template <class T>
+struct InMemory {
+  const T* p;
+  __device__ __forceinline__ const T& get() const { return *p; }
+};
+
 // Compacted ray record: direction + start distance, and (view, pixel, n).
 struct RayMeta {
   int view;

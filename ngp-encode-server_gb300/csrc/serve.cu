@@ -7,16 +7,22 @@
 // (src/base/video/frame_queue.cc:11-39, frame_map.cc:12-53).  Here:
 //  - nes_submit admits a request (mono or stereo, any resolution) if its
 //    device output slots fit the memory budget and the pending queue has
-//    room; otherwise it is dropped and counted (no silent stall);
+//    room, carving them out of an output arena allocated once at creation;
+//    otherwise it is dropped and counted (no silent stall, and no device
+//    allocation on the request path);
 //  - a scheduler thread forms a batch from the pending requests (FIFO, up to
 //    max_batch_pixels) whenever one of max_inflight_batches stream slots is
 //    free, so requests arriving while others run join the next batch and
 //    overlap them on the device;
 //  - a batch is one ray queue over all its views: ray generation with
-//    compaction, one persistent march, then per view RGB24 quantisation,
-//    YUV420P conversion and depth packing into the request's device slots;
-//    the whole batch is captured as a CUDA graph and replayed per batch
-//    shape (cudaGraphExecUpdate swaps in the new poses and pointers);
+//    compaction, one persistent march, then one fused launch for every
+//    view's RGB24 quantisation, YUV420P conversion and depth packing into the
+//    request's output slots;
+//  - every kernel reads the batch from a device-side descriptor (views,
+//    poses, output pointers) that the first node copies from the slot's
+//    pinned host copy, and every grid is fixed by max_batch_pixels, so each
+//    slot's CUDA graph is captured and instantiated once at creation and
+//    replayed for every batch of any shape;
 //  - a completion thread waits for each batch's event in launch order and
 //    publishes its requests with their pose->YUV latency.
 #include <cuda_runtime.h>
@@ -27,7 +33,6 @@
 #include <deque>
 #include <map>
 #include <mutex>
-#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -79,7 +84,8 @@ struct Req {
   nes_request r{};
   ViewPlanes planes[2];
   size_t bytes = 0;
-  uint8_t* dev = nullptr;  // output slots (allocated when the batch forms)
+  uint8_t* dev = nullptr;  // output slots, carved from the arena at admission
+  size_t arena_off = 0;
   ReqState state = ReqState::Pending;
   int status = NES_OK;
   Clock::time_point t_submit, t_done;
@@ -88,20 +94,69 @@ struct Req {
   uint32_t batch_requests = 0, batch_views = 0;
 };
 
+// The batch descriptor every kernel of a slot reads at run time.
+struct BatchDesc {
+  ViewBatch vb;
+  FrameBatch fb;
+};
+
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
   DevScratch scratch;
   float* rgb = nullptr;
   float* depth = nullptr;
-  uint8_t* rgb8 = nullptr;
+  uint8_t* warm = nullptr;         // outputs of the creation-time warm-up batch
   uint32_t* h_counters = nullptr;  // pinned copy of the batch's counters
+  BatchDesc* h_desc = nullptr;     // pinned: written by the host per batch
+  BatchDesc* d_desc = nullptr;     // device: copied from h_desc by the batch's first node
+  cudaGraphExec_t graph = nullptr; // the slot's batch, instantiated once
   bool busy = false;
   uint64_t batch_id = 0;
   std::vector<uint64_t> tickets;
   uint64_t pixels = 0;
   Clock::time_point t_launch;
-  std::map<std::string, cudaGraphExec_t> graphs;
+};
+
+// First-fit free list over one device allocation: request outputs are
+// carved out at admission and handed back at release, so serving never
+// calls the CUDA allocator after creation.  Offsets and sizes are multiples
+// of 256 bytes; neighbouring free ranges are merged.
+class Arena {
+ public:
+  static constexpr size_t kNone = ~size_t(0);
+  void reset(size_t bytes) {
+    free_.clear();
+    if (bytes) free_[0] = bytes;
+  }
+  size_t alloc(size_t bytes) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < bytes) continue;
+      const size_t off = it->first, rest = it->second - bytes;
+      free_.erase(it);
+      if (rest) free_[off + bytes] = rest;
+      return off;
+    }
+    return kNone;
+  }
+  void release(size_t off, size_t bytes) {
+    auto next = free_.lower_bound(off);
+    if (next != free_.end() && off + bytes == next->first) {
+      bytes += next->second;
+      next = free_.erase(next);
+    }
+    if (next != free_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        prev->second += bytes;
+        return;
+      }
+    }
+    free_[off] = bytes;
+  }
+
+ private:
+  std::map<size_t, size_t> free_;  // offset -> size
 };
 
 }  // namespace
@@ -110,8 +165,9 @@ struct nes_server {
   nes_ctx* ctx = nullptr;
   nes_server_config cfg{};
   std::vector<Slot> slots;
-  cudaStream_t release_stream = nullptr;
   uint64_t fixed_bytes = 0;
+  uint8_t* arena_base = nullptr;  // device memory of the output arena
+  Arena arena;                    // guarded by mu
 
   std::mutex mu;
   std::condition_variable cv_sched, cv_done;
@@ -128,10 +184,6 @@ struct nes_server {
   uint64_t pending_pixels = 0, inflight_pixels = 0;
   double rate_px_per_ms = 0.0, delay_scale = 1.0;
   Clock::time_point last_done;
-  // Batch shapes seen so far (scheduler thread only): a shape is launched
-  // directly the first time and captured as a graph once it recurs, so
-  // one-off mixes of resolutions cost no graph instantiation.
-  std::unordered_map<std::string, uint32_t> shape_seen;
   bool stop = false;
   nes_server_stats stats{};
   std::thread sched, comp;
@@ -145,87 +197,69 @@ namespace {
     if (e_ != cudaSuccess) return NES_EIO; \
   } while (0)
 
-// Queues one batch on the slot's stream (inside or outside stream capture).
-int enqueue_batch(nes_server* s, Slot& sl, const ViewBatch& vb, const std::vector<Req*>& reqs) {
+// Queues one batch on the slot's stream, inside or outside stream capture.
+// Nothing here depends on the batch: the kernels read it from d_desc.
+int enqueue_batch(nes_server* s, Slot& sl) {
   nes_ctx* c = s->ctx;
-  SRV_CUDA(enqueue_march(vb, c->scene, sl.scratch, c->cfg.precision, c->num_sms, sl.st));
-  int vi = 0;
-  for (Req* r : reqs) {
-    for (uint32_t k = 0; k < r->r.nviews; ++k, ++vi) {
-      const DevView& V = vb.v[vi];
-      const ViewPlanes& p = r->planes[k];
-      const size_t px = (size_t)p.w * p.h;
-      uint8_t* rgb8 = sl.rgb8 + (size_t)(V.rgb - sl.rgb);  // same pixel offset, 1 byte per channel
-      SRV_CUDA(launch_rgb_to_rgb24(V.rgb, px * 3, rgb8, sl.st));
-      SRV_CUDA(launch_rgb24_to_yuv420p(rgb8, (int)p.w, (int)p.h, (int)p.w * 3, r->dev + p.off_y, r->dev + p.off_u,
-                                       r->dev + p.off_v, p.ls, sl.st));
-      SRV_CUDA(launch_depth_pack_u16mm(V.depth, px, reinterpret_cast<uint16_t*>(r->dev + p.off_d), sl.st));
-    }
-  }
+  const uint32_t P = s->cfg.max_batch_pixels;
+  SRV_CUDA(cudaMemcpyAsync(sl.d_desc, sl.h_desc, sizeof(BatchDesc), cudaMemcpyHostToDevice, sl.st));
+  SRV_CUDA(cudaMemsetAsync(sl.scratch.counters, 0, kCtrWords * sizeof(uint32_t), sl.st));
+  SRV_CUDA(launch_raygen(&sl.d_desc->vb, P, c->num_sms, sl.scratch, sl.st));
+  if (c->cfg.precision == NES_PREC_FP16_TC)
+    SRV_CUDA(launch_march_tc(&sl.d_desc->vb, c->scene, sl.scratch, c->num_sms, sl.st));
+  else
+    SRV_CUDA(launch_march_fp32(&sl.d_desc->vb, c->scene, sl.scratch, c->num_sms, sl.st));
+  SRV_CUDA(launch_frame_out(&sl.d_desc->fb, c->num_sms, sl.st));
   SRV_CUDA(cudaMemcpyAsync(sl.h_counters, sl.scratch.counters, kCtrWords * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                            sl.st));
   return NES_OK;
 }
 
-std::string shape_key(const std::vector<Req*>& reqs) {
-  std::string k;
-  for (Req* r : reqs)
-    for (uint32_t v = 0; v < r->r.nviews; ++v)
-      k += std::to_string(r->planes[v].w) + "x" + std::to_string(r->planes[v].h) + ";";
-  return k;
+// Fills the slot's pinned descriptor for a batch of views whose FP32 render
+// goes to the slot's buffers and whose frames go to the given planes.
+int fill_desc(nes_server* s, Slot& sl, const nes_view* views, const ViewPlanes* planes, uint8_t* const* out_base,
+              int n) {
+  float* rgbp[kMaxViews];
+  float* depp[kMaxViews];
+  uint64_t px = 0;
+  for (int i = 0; i < n; ++i) {
+    rgbp[i] = sl.rgb + 3 * px;
+    depp[i] = sl.depth + px;
+    px += (uint64_t)planes[i].w * planes[i].h;
+  }
+  uint64_t npx = 0;
+  const int rc = fill_view_batch(views, n, rgbp, depp, s->cfg.max_batch_pixels, &sl.h_desc->vb, &npx);
+  if (rc != NES_OK) return rc;
+  FrameBatch& fb = sl.h_desc->fb;
+  std::memset(&fb, 0, sizeof(fb));
+  fb.n = n;
+  for (int i = 0; i < n; ++i) {
+    const ViewPlanes& p = planes[i];
+    FrameOut& F = fb.f[i];
+    F.rgb = rgbp[i];
+    F.depth = depp[i];
+    F.y = out_base[i] + p.off_y;
+    F.u = out_base[i] + p.off_u;
+    F.v = out_base[i] + p.off_v;
+    F.depth_mm = reinterpret_cast<uint16_t*>(out_base[i] + p.off_d);
+    F.w = (int)p.w;
+    F.h = (int)p.h;
+    F.ls0 = p.ls[0];
+    F.ls1 = p.ls[1];
+    F.ls2 = p.ls[2];
+  }
+  frame_batch_index(&fb);
+  return NES_OK;
 }
 
-// Launches a batch: plain launches (graphs off, or a shape's first
-// occurrence), or capture + instantiate/update + replay.  Runs outside the
-// server lock (the scheduler thread is its only caller); graph counters go to
-// *inst / *upd.
-int launch_batch(nes_server* s, Slot& sl, const ViewBatch& vb, const std::vector<Req*>& reqs, uint64_t* inst,
-                 uint64_t* upd) {
-  for (Req* r : reqs) SRV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&r->dev), r->bytes, sl.st));
-  const std::string key = shape_key(reqs);
-  if (s->shape_seen.size() > 4096) s->shape_seen.clear();  // bounded memory for endless mixes
-  const uint32_t seen = ++s->shape_seen[key];
-  if (sl.graphs.size() > 256) {  // likewise for the executable graphs of this slot
-    for (auto& kv : sl.graphs) cudaGraphExecDestroy(kv.second);
-    sl.graphs.clear();
-  }
-  if (!s->cfg.use_graphs || (seen < 2 && sl.graphs.find(key) == sl.graphs.end())) {
-    const int rc = enqueue_batch(s, sl, vb, reqs);
-    if (rc != NES_OK) return rc;
+// Launches the batch whose descriptor is in sl.h_desc: the slot's graph, or
+// the same launches one by one when graphs are off.
+int launch_batch(nes_server* s, Slot& sl) {
+  if (sl.graph) {
+    SRV_CUDA(cudaGraphLaunch(sl.graph, sl.st));
   } else {
-    SRV_CUDA(cudaStreamBeginCapture(sl.st, cudaStreamCaptureModeThreadLocal));
-    const int rc = enqueue_batch(s, sl, vb, reqs);
-    cudaGraph_t g = nullptr;
-    const cudaError_t ec = cudaStreamEndCapture(sl.st, &g);
-    if (rc != NES_OK || ec != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      return rc != NES_OK ? rc : NES_EIO;
-    }
-    auto it = sl.graphs.find(key);
-    bool ok = false;
-    if (it != sl.graphs.end()) {
-      cudaGraphExecUpdateResultInfo info;
-      if (cudaGraphExecUpdate(it->second, g, &info) == cudaSuccess) {
-        ok = true;
-        ++*upd;
-      } else {
-        cudaGetLastError();
-        cudaGraphExecDestroy(it->second);
-        sl.graphs.erase(it);
-      }
-    }
-    if (!ok) {
-      cudaGraphExec_t ex = nullptr;
-      if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
-        cudaGraphDestroy(g);
-        return NES_EIO;
-      }
-      sl.graphs[key] = ex;
-      ++*inst;
-    }
-    const cudaError_t el = cudaGraphLaunch(sl.graphs[key], sl.st);
-    cudaGraphDestroy(g);
-    if (el != cudaSuccess) return NES_EIO;
+    const int rc = enqueue_batch(s, sl);
+    if (rc != NES_OK) return rc;
   }
   SRV_CUDA(cudaEventRecord(sl.done, sl.st));
   return NES_OK;
@@ -251,21 +285,22 @@ void scheduler_main(nes_server* s) {
     // FIFO batch formation up to the pixel and view limits.
     std::vector<Req*> batch;
     std::vector<uint64_t> tickets;
-    std::vector<nes_view> views;
-    std::vector<float*> rgbp, depp;
+    nes_view views[kMaxViews];
+    ViewPlanes planes[kMaxViews];
+    uint8_t* outs[kMaxViews];
+    int nv = 0;
     uint64_t pixels = 0;
     while (!s->pending.empty()) {
       Req& r = s->reqs[s->pending.front()];
       uint64_t px = 0;
       for (uint32_t v = 0; v < r.r.nviews; ++v) px += (uint64_t)r.planes[v].w * r.planes[v].h;
-      if (!batch.empty() && (pixels + px > s->cfg.max_batch_pixels || views.size() + r.r.nviews > (size_t)kMaxViews))
-        break;
-      for (uint32_t v = 0; v < r.r.nviews; ++v) {
-        views.push_back(r.r.views[v]);
-        rgbp.push_back(sl.rgb + 3 * (pixels));
-        depp.push_back(sl.depth + pixels);
-        pixels += (uint64_t)r.planes[v].w * r.planes[v].h;
+      if (!batch.empty() && (pixels + px > s->cfg.max_batch_pixels || nv + (int)r.r.nviews > kMaxViews)) break;
+      for (uint32_t v = 0; v < r.r.nviews; ++v, ++nv) {
+        views[nv] = r.r.views[v];
+        planes[nv] = r.planes[v];
+        outs[nv] = r.dev;
       }
+      pixels += px;
       tickets.push_back(s->pending.front());
       batch.push_back(&r);
       s->pending.pop_front();
@@ -277,7 +312,7 @@ void scheduler_main(nes_server* s) {
       r->state = ReqState::Running;
       r->batch_id = bid;
       r->batch_requests = (uint32_t)batch.size();
-      r->batch_views = (uint32_t)views.size();
+      r->batch_views = (uint32_t)nv;
     }
     sl.busy = true;
     sl.batch_id = bid;
@@ -286,18 +321,17 @@ void scheduler_main(nes_server* s) {
     sl.t_launch = Clock::now();
     lk.unlock();
 
-    ViewBatch vb;
-    uint64_t npx = 0;
-    int rc = fill_view_batch(views.data(), (int)views.size(), rgbp.data(), depp.data(), s->cfg.max_batch_pixels, &vb,
-                             &npx);
-    uint64_t inst = 0, upd = 0;
-    if (rc == NES_OK) rc = launch_batch(s, sl, vb, batch, &inst, &upd);
+    // The slot is idle (its last batch completed), so its pinned descriptor
+    // can be rewritten.
+    int rc = fill_desc(s, sl, views, planes, outs, nv);
+    if (rc == NES_OK) rc = launch_batch(s, sl);
+    // A failed launch may have queued part of the batch: let that finish
+    // before the requests (and their output slots) are handed back.
+    if (rc != NES_OK) cudaStreamSynchronize(sl.st);
 
     lk.lock();
     s->stats.batches++;
-    s->stats.graph_instantiations += inst;
-    s->stats.graph_updates += upd;
-    if (rc != NES_OK) {  // publish the failure; nothing is in flight on this slot
+    if (rc != NES_OK) {  // publish the failure; the slot's stream is idle
       s->inflight_pixels -= sl.pixels;
       for (uint64_t t : tickets) {
         Req& r = s->reqs[t];
@@ -365,18 +399,22 @@ void completion_main(nes_server* s) {
 void destroy_slots(nes_server* s) {
   for (Slot& sl : s->slots) {
     if (sl.st) cudaStreamSynchronize(sl.st);
-    for (auto& kv : sl.graphs) cudaGraphExecDestroy(kv.second);
+    if (sl.graph) cudaGraphExecDestroy(sl.graph);
     cudaFree(sl.scratch.ray_dt);
     cudaFree(sl.scratch.ray_meta);
     cudaFree(sl.scratch.counters);
     cudaFree(sl.rgb);
     cudaFree(sl.depth);
-    cudaFree(sl.rgb8);
+    cudaFree(sl.warm);
+    cudaFree(sl.d_desc);
+    if (sl.h_desc) cudaFreeHost(sl.h_desc);
     if (sl.h_counters) cudaFreeHost(sl.h_counters);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.st) cudaStreamDestroy(sl.st);
   }
   s->slots.clear();
+  cudaFree(s->arena_base);
+  s->arena_base = nullptr;
 }
 
 }  // namespace
@@ -407,8 +445,9 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
   s->ctx = ctx;
   s->cfg = *cfg;
   const size_t P = cfg->max_batch_pixels;
-  // Per slot: 32 B ray record + 16 B FP32 colour/depth + 3 B RGB24 per pixel.
-  s->fixed_bytes = (uint64_t)cfg->max_inflight_batches * (P * (32 + 16 + 3) + 4096);
+  // Per slot: 32 B ray record + 16 B FP32 colour/depth per pixel, the
+  // descriptor and the warm-up outputs.
+  s->fixed_bytes = (uint64_t)cfg->max_inflight_batches * (P * (32 + 16) + sizeof(BatchDesc) + kWarmupBytes + 4096);
   if (s->fixed_bytes > cfg->hbm_budget_bytes) {
     delete s;
     return NES_ENOMEM;
@@ -417,10 +456,13 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
   s->slots.resize(cfg->max_inflight_batches);
   auto fail = [&](int code) {
     destroy_slots(s);
-    if (s->release_stream) cudaStreamDestroy(s->release_stream);
     delete s;
     return code;
   };
+  // The output arena: the rest of the budget, reserved up front.
+  const size_t arena_bytes = (size_t)(cfg->hbm_budget_bytes - s->fixed_bytes) / 256 * 256;
+  if (arena_bytes && cudaMalloc(&s->arena_base, arena_bytes) != cudaSuccess) return fail(NES_ENOMEM);
+  s->arena.reset(arena_bytes);
   for (Slot& sl : s->slots) {
     if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess) return fail(NES_EIO);
     if (cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming | cudaEventBlockingSync) != cudaSuccess)
@@ -431,18 +473,14 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
     sl.scratch.max_rays = (uint32_t)P;
     if (cudaMalloc(&sl.rgb, P * 3 * sizeof(float)) != cudaSuccess) return fail(NES_ENOMEM);
     if (cudaMalloc(&sl.depth, P * sizeof(float)) != cudaSuccess) return fail(NES_ENOMEM);
-    if (cudaMalloc(&sl.rgb8, P * 3 > kWarmupBytes ? P * 3 : kWarmupBytes) != cudaSuccess) return fail(NES_ENOMEM);
+    if (cudaMalloc(&sl.warm, kWarmupBytes) != cudaSuccess) return fail(NES_ENOMEM);
+    if (cudaMalloc(&sl.d_desc, sizeof(BatchDesc)) != cudaSuccess) return fail(NES_ENOMEM);
+    if (cudaMallocHost(&sl.h_desc, sizeof(BatchDesc)) != cudaSuccess) return fail(NES_ENOMEM);
     if (cudaMallocHost(&sl.h_counters, kCtrWords * sizeof(uint32_t)) != cudaSuccess) return fail(NES_ENOMEM);
   }
-  if (cudaStreamCreateWithFlags(&s->release_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(NES_EIO);
-  // Keep freed output slots in the pool for reuse instead of returning them.
-  cudaMemPool_t pool;
-  if (cudaDeviceGetDefaultMemPool(&pool, ctx->cfg.device) == cudaSuccess) {
-    uint64_t thr = cfg->hbm_budget_bytes;
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-  }
-  // Warm-up batch outside capture so every kernel's module is loaded and its
-  // attributes set before the first capture.
+  // Per slot: one warm-up batch of plain launches (loads every kernel's
+  // module and sets its attributes outside capture), then the capture and
+  // the one instantiation of the slot's graph.
   {
     nes_view v;
     std::memset(&v, 0, sizeof(v));
@@ -451,21 +489,29 @@ int nes_server_create(nes_ctx* ctx, const nes_server_config* cfg, nes_server** o
     v.width = v.height = kWarmupSide;
     v.focal_px = 0.5f * kWarmupSide;
     for (Slot& sl : s->slots) {
-      ViewBatch vb;
-      uint64_t px = 0;
-      float* rgb[1] = {sl.rgb};
-      float* dep[1] = {sl.depth};
-      if (fill_view_batch(&v, 1, rgb, dep, P, &vb, &px) != NES_OK) return fail(NES_EIO);
-      if (enqueue_march(vb, ctx->scene, sl.scratch, ctx->cfg.precision, ctx->num_sms, sl.st) != cudaSuccess)
-        return fail(NES_EIO);
-      const int ls[3] = {32, 32, 32};
-      const size_t wpx = kWarmupSide * kWarmupSide;
-      if (launch_rgb_to_rgb24(sl.rgb, wpx * 3, sl.rgb8, sl.st) != cudaSuccess ||
-          launch_rgb24_to_yuv420p(sl.rgb8, kWarmupSide, kWarmupSide, 3 * kWarmupSide, sl.rgb8 + 256, sl.rgb8 + 512,
-                                  sl.rgb8 + 768, ls, sl.st) != cudaSuccess ||
-          launch_depth_pack_u16mm(sl.depth, wpx, reinterpret_cast<uint16_t*>(sl.rgb8 + 1024), sl.st) != cudaSuccess)
-        return fail(NES_EIO);
+      ViewPlanes p = plan_view(kWarmupSide, kWarmupSide, 0);
+      uint8_t* base[1] = {sl.warm};
+      if (p.bytes > kWarmupBytes) return fail(NES_EIO);
+      if (fill_desc(s, sl, &v, &p, base, 1) != NES_OK) return fail(NES_EIO);
+      if (enqueue_batch(s, sl) != NES_OK) return fail(NES_EIO);
       if (cudaStreamSynchronize(sl.st) != cudaSuccess) return fail(NES_EIO);
+      if (cfg->use_graphs) {
+        if (cudaStreamBeginCapture(sl.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return fail(NES_EIO);
+        const int rc = enqueue_batch(s, sl);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(sl.st, &g);
+        if (rc != NES_OK || ec != cudaSuccess) {
+          if (g) cudaGraphDestroy(g);
+          return fail(NES_EIO);
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&sl.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+          sl.graph = nullptr;
+          return fail(NES_EIO);
+        }
+        s->stats.graph_instantiations++;
+      }
     }
   }
   s->sched = std::thread(scheduler_main, s);
@@ -479,6 +525,15 @@ void nes_server_destroy(nes_server* s) {
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
+    // Requests never batched finish now with an error, so no waiter sleeps
+    // on a request that will not run.
+    for (uint64_t t : s->pending) {
+      Req& r = s->reqs[t];
+      r.state = ReqState::Done;
+      r.status = NES_EIO;
+      r.t_done = Clock::now();
+    }
+    s->pending.clear();
   }
   s->cv_sched.notify_all();
   s->cv_done.notify_all();
@@ -486,14 +541,9 @@ void nes_server_destroy(nes_server* s) {
   if (s->comp.joinable()) s->comp.join();
   cudaSetDevice(s->ctx->cfg.device);
   // A batch launched while the stop was being set may still run (the
-  // completion thread can have left first): its outputs are freed after it.
-  for (Slot& sl : s->slots)
-    if (sl.st) cudaStreamSynchronize(sl.st);
-  for (auto& kv : s->reqs)
-    if (kv.second.dev) cudaFreeAsync(kv.second.dev, s->release_stream);
-  cudaStreamSynchronize(s->release_stream);
+  // completion thread can have left first): its outputs live in the arena,
+  // which destroy_slots frees after synchronising every slot stream.
   destroy_slots(s);
-  cudaStreamDestroy(s->release_stream);
   delete s;
 }
 
@@ -523,11 +573,16 @@ int nes_submit(nes_server* s, const nes_request* req, uint64_t* ticket) {
   const bool late = s->cfg.max_queue_ms > 0.0f &&
                     (s->rate_px_per_ms > 0.0 ? pred * s->delay_scale > s->cfg.max_queue_ms
                                              : s->pending_pixels + s->inflight_pixels + px > s->cfg.max_batch_pixels);
-  if (s->pending.size() >= s->cfg.max_pending || late ||
-      s->stats.budget_used_bytes + r.bytes > s->cfg.hbm_budget_bytes) {
+  size_t off = Arena::kNone;
+  if (s->pending.size() < s->cfg.max_pending && !late &&
+      s->stats.budget_used_bytes + r.bytes <= s->cfg.hbm_budget_bytes)
+    off = s->arena.alloc(r.bytes);
+  if (off == Arena::kNone) {
     s->stats.rejected++;
     return NES_EAGAIN;
   }
+  r.arena_off = off;
+  r.dev = s->arena_base + off;
   s->pending_pixels += px;
   s->stats.submitted++;
   s->stats.budget_used_bytes += r.bytes;
@@ -585,10 +640,9 @@ int nes_release(nes_server* s, uint64_t ticket) {
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end() || it->second.state != ReqState::Done) return NES_EINVAL;
-  if (it->second.dev) {
-    cudaSetDevice(s->ctx->cfg.device);
-    if (cudaFreeAsync(it->second.dev, s->release_stream) != cudaSuccess) return NES_EIO;
-  }
+  // Done means the request's batch has finished on the GPU (or its slot's
+  // stream was synchronised after a failed launch): the slots are free.
+  if (it->second.dev) s->arena.release(it->second.arena_off, it->second.bytes);
   s->stats.budget_used_bytes -= it->second.bytes;
   s->reqs.erase(it);
   s->cv_sched.notify_one();

@@ -108,6 +108,8 @@ _SIGS = {
     "nes_render": (_I, [_P, _P, _SZ, _P, _SZ, ctypes.POINTER(_SZ)]),
     "nes_render_views": (_I, [_P, _P, _I, _P, _P, _P]),
     "nes_render_yuv": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(_I), _P]),
+    "nes_render_yuv_views": (_I, [_P, _P, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                  ctypes.POINTER(_I), ctypes.POINTER(_P)]),
     "nes_rgb24_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
     "nes_gray8_to_yuv420p": (_I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
     "nes_depth_pack_u16mm": (_I, [_P, _SZ, _P, _P]),
@@ -275,6 +277,16 @@ class Renderer:
         lsa = (_I * 3)(*ls)
         check(self.lib.nes_render_yuv(self.h, ctypes.byref(view), _P(y_ptr), _P(u_ptr), _P(v_ptr), lsa,
                                       _P(depth_ptr) if depth_ptr else None), "nes_render_yuv")
+
+    def render_yuv_views(self, views, y_ptrs, u_ptrs, v_ptrs, ls, depth_ptrs=None):
+        """Pose -> YUV for several views of one size (e.g. a stereo pair) in
+        one batch, planes copied to the given host buffers."""
+        nv = len(views)
+        arr = (NesView * nv)(*views)
+        lsa = (_I * 3)(*ls)
+        dep = _ptrs(depth_ptrs) if depth_ptrs else None
+        check(self.lib.nes_render_yuv_views(self.h, arr, nv, _ptrs(y_ptrs), _ptrs(u_ptrs), _ptrs(v_ptrs), lsa, dep),
+              "nes_render_yuv_views")
 
     def scene_param(self, which, count):
         import numpy as np

@@ -173,3 +173,29 @@ def test_render_yuv_end_to_end(r32, cuda, nes_lib, oracle_mod):
     oy, ou, ov = oracle_mod.rgb24_to_yuv420p(rgb24, W, H, W * 3, ls)
     assert np.array_equal(y.numpy(), oy) and np.array_equal(u.numpy(), ou) and np.array_equal(v.numpy(), ov)
     assert np.array_equal(dmm.numpy().view(np.uint16), oracle_mod.depth_pack_u16mm(dep.cpu().numpy()))
+
+
+def test_render_yuv_views_stereo_matches_single_views(rtc, cuda, nes_lib):
+    """A stereo pair through nes_render_yuv_views (one batch, one march, one
+    frame-output launch) gives each eye the bytes nes_render_yuv gives it
+    alone."""
+    torch = cuda
+    W, H = 640, 366  # odd chroma height
+    M = nes_lib.shell_poses(9, 1, 1.2, 2.0)[0]
+    f = nes_lib.focal_from_fov(W, 100.0)
+    views = [nes_lib.make_view(m, W, H, f) for m in nes_lib.stereo_pair(M, 0.063)]
+    ls = nes_lib.linesizes(W)
+    ch = (H + 1) // 2
+
+    def bufs():
+        return [torch.zeros(n, dtype=torch.uint8).pin_memory() for n in (ls[0] * H, ls[1] * ch, ls[2] * ch)] + \
+               [torch.zeros(W * H, dtype=torch.int16).pin_memory()]
+
+    pair = [bufs(), bufs()]
+    rtc.render_yuv_views(views, [b[0].data_ptr() for b in pair], [b[1].data_ptr() for b in pair],
+                         [b[2].data_ptr() for b in pair], ls, [b[3].data_ptr() for b in pair])
+    for v, got in zip(views, pair):
+        one = bufs()
+        rtc.render_yuv(v, one[0].data_ptr(), one[1].data_ptr(), one[2].data_ptr(), ls, one[3].data_ptr())
+        for a, b in zip(got, one):
+            assert np.array_equal(a.numpy(), b.numpy())
