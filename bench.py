@@ -70,6 +70,7 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-extras", action="store_true", help="skip the stereo and serving sections")
     p.add_argument("--serve-seconds", type=float, default=3.0)
+    p.add_argument("--stereo-poses", type=int, default=200, help="poses of the stereo precision-form section")
     p.add_argument("--train-steps", type=int, default=20, help="refit steps timed in the training section")
     p.add_argument("--train-batch", type=int, default=1 << 18, help="rays per refit step")
     p.add_argument("--section", choices=["all", "training"], default="all",
@@ -281,7 +282,15 @@ def run_ours(args):
             res = {"total_ms": total_ms, "ms_per_step": total_ms / args.steps,
                    "mrays": job_mrays(world, W * H, args.steps, total_ms),
                    "march_ms": statistics.mean(march_ms), "raygen_ms": statistics.mean(raygen_ms),
-                   "samples_per_step": statistics.mean(samples), "clocks": clk.summary()}
+                   "samples_per_step": statistics.mean(samples), "clocks": clk.summary(),
+                   # hitting rays of the last timed request (a miss has depth 0)
+                   "rays_per_step": int((dep > 0).sum().item())}
+            if prec == nes.PREC_FP16_TC and rank == 0:
+                # The replay covers the timed steps' poses in turn, one per replay.
+                res["gather"] = measure_gather_ceilings(r, [views[0]], flush, stream, dev)
+                res["gather"]["replay_pose"] = 0
+                res["march_ms_pose0"] = march_ms[0]
+                res["samples_pose0"] = samples[0]
 
             # End to end through the host-buffer C-ABI call.
             ke = args.e2e_steps or args.steps
@@ -319,7 +328,7 @@ def run_ours(args):
     head = results[renderer_used]
     hbm, tf_burst, tf_sust, src = load_peaks()
     kind = "fp16" if renderer_used == nes.PREC_FP16_TC else "fp32"
-    achieved = head["samples_per_step"] * FLOP_PER_SAMPLE / (head["march_ms"] / 1e3) / 1e12
+    roof = roofline_terms(head, kind, tf_sust, src, hbm)
     line = {
         "metric": "Mrays/s (pose->YUV render, all pixels)", "value": round(head["mrays"], 3), "unit": "Mrays/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -332,21 +341,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": head["e2e"]["h2d"], "d2h_bytes_per_step": head["e2e"]["d2h"],
                 "p50_ms": round(head["e2e"]["p50_ms"], 3), "p99_ms": round(head["e2e"]["p99_ms"], 3)},
         "gpu_launches": 5 * args.steps,
-        "roofline": {"bound": "tensor", "achieved": round(achieved, 3), "peak": tf_sust, "unit": "TFLOP/s",
-                     "frac": round(achieved / tf_sust, 5),
-                     "traffic": DRAM_BYTES_PER_LAUNCH[kind] if (W, H) == (1920, 1080) else None,
-                     "traffic_note": "DRAM bytes per launch (ncu); the FP16 table (32 MiB) and the corner "
-                                     "records of levels 0-6 (70 MB) stay in L2, those of levels 7-9 (1.23 GB) "
-                                     "come from HBM; the 512 B/sample of gathers are served mostly by L1/L2",
-                     "limiter": "hash-table gathers: L1 data pipe at 69-73% of its wavefront rate, ALU 40%, "
-                                "tensor pipe 11% (ncu capture of one 1920x1080 march launch)",
-                     "l1_wavefront_frac": L1_WAVEFRONT_FRAC.get(kind),
-                     "kernel": "march", "peak_source": src + " bf16 sustained",
-                     "march_ms": round(head["march_ms"], 3), "raygen_ms": round(head["raygen_ms"], 4),
-                     "samples_per_step": int(head["samples_per_step"]),
-                     "msamples_per_s": round(head["samples_per_step"] / (head["march_ms"] / 1e3) / 1e6, 1),
-                     "frames_per_s": round(1e3 / head["ms_per_step"], 2),
-                     "gather_gbs": round(head["samples_per_step"] * GATHER_BYTES[kind] / (head["march_ms"] / 1e3) / 1e9, 1)},
+        "roofline": roof,
         "clocks": head["clocks"],
         "paths": {("fp16_tc" if k == nes.PREC_FP16_TC else "fp32"):
                   ({"mrays": round(v["mrays"], 3), "ms_per_step": round(v["ms_per_step"], 3),
@@ -354,7 +349,7 @@ def run_ours(args):
                    if "mrays" in v else v) for k, v in results.items()},
     }
     if world == 1 and not args.no_extras:
-        line["stereo"] = run_stereo(dev, min(args.steps, 20))
+        line["stereo"] = run_stereo(dev, nposes=args.stereo_poses)
         line["serving"] = run_serving(dev, args.serve_seconds)
         line["serving_delay_bounded"] = run_serving(dev, args.serve_seconds, max_queue_ms=100.0)
         line["glue"] = run_glue(dev, {"hbm_gbs": hbm})
@@ -365,6 +360,106 @@ def run_ours(args):
         cb = cpu_baseline_with_parity(dev, poses[0], per)
         line["cpu_baseline"] = cb
     print(json.dumps(line), flush=True)
+
+
+def roofline_terms(head, kind, tf_sust, src, hbm):
+    """The march's two roofline terms per launch: the MLP contraction
+    (18,688 FLOP per sample) against the measured bf16 tensor peak, and the
+    gather stream (512 B per sample) against the march's own load stream
+    replayed on this device with no arithmetic.  `bound` names the term
+    with the larger floor; achieved / peak / frac are that term's."""
+    ms, n = head["march_ms"], head["samples_per_step"]
+    tflops = n * FLOP_PER_SAMPLE / (ms / 1e3) / 1e12
+    t_tensor = n * FLOP_PER_SAMPLE / (tf_sust * 1e12) * 1e3
+    out = {"kernel": "march", "march_ms": round(ms, 3), "raygen_ms": round(head["raygen_ms"], 4),
+           "samples_per_step": int(n), "msamples_per_s": round(n / (ms / 1e3) / 1e6, 1),
+           "frames_per_s": round(1e3 / head["ms_per_step"], 2),
+           "tensor": {"achieved": round(tflops, 3), "peak": tf_sust, "unit": "TFLOP/s",
+                      "frac": round(tflops / tf_sust, 5), "floor_ms": round(t_tensor, 3),
+                      "peak_source": src + " bf16 sustained (MEASURED_PEAKS.json)",
+                      "per_unit": "18,688 FLOP per sample (2 x 9,344 MLP multiply-adds)"},
+           "tensor_frac": round(tflops / tf_sust, 5)}
+    gbytes = n * GATHER_BYTES[kind]
+    out["gather_achieved_gbs"] = round(gbytes / (ms / 1e3) / 1e9, 1)
+    g = head.get("gather")
+    if g:
+        # The replay ran on pose 0; its floor scales to the mean step by samples.
+        t_replay = g["replay_ms"] * n / head["samples_pose0"]
+        peak = gbytes / (t_replay / 1e3) / 1e9
+        out["gather"] = {"achieved": out["gather_achieved_gbs"], "peak": round(peak, 1), "unit": "GB/s",
+                         "frac": round(t_replay / ms, 4), "floor_ms": round(t_replay, 3),
+                         "peak_source": "measured in this run: the march's own load stream replayed with no "
+                                        "interpolation, MLP or compositing (nes_probe_gather_replay, pose 0, "
+                                        "L2 flushed, scaled to the mean step's samples)",
+                         "per_unit": "512 B per sample (16 levels x 8 corners x 2 FP16 features)",
+                         "random_gathers": {k: v for k, v in g.items() if k.startswith("random")}}
+        out["gather_frac"] = out["gather"]["frac"]
+        bound = "gather" if t_replay > t_tensor else "tensor"
+    else:
+        bound = "tensor"
+    term = out["gather"] if bound == "gather" else out["tensor"]
+    out.update({"bound": bound, "achieved": term["achieved"], "peak": term["peak"], "unit": term["unit"],
+                "frac": term["frac"]})
+    traffic = DRAM_BYTES_PER_LAUNCH.get(kind) if (W, H) == (1920, 1080) else None
+    rays = head.get("rays_per_step") or W * H
+    algo = (16 << 19) * (2 if kind == "fp16" else 4) * 2 + rays * 32 + W * H * 16
+    out.update({"traffic": traffic, "traffic_source": DRAM_SOURCE if traffic else None,
+                "algorithmic_hbm_bytes": int(algo),
+                "traffic_ratio": round(traffic / algo, 1) if traffic else None,
+                "traffic_note": "algorithmic HBM bytes: the table read once, the ray list (32 B per hitting ray) "
+                                "and the FP32 RGB + depth written (16 B per pixel); the measured excess is the "
+                                "per-cell corner records of levels 7-9 (1.23 GB copy of table entries, read "
+                                "from HBM because they exceed L2)",
+                "hbm_peak_gbs": hbm,
+                "limiter": "hash-table gathers: L1 data pipe at 69-73% of its wavefront rate, ALU 40%, "
+                           "tensor pipe 11% (ncu capture of one 1920x1080 march launch)",
+                "l1_wavefront_frac": L1_WAVEFRONT_FRAC.get(kind)})
+    return out
+
+
+def measure_gather_ceilings(r, views, flush, stream, dev, reps=5):
+    """The gather term of the march's roofline, measured on this device:
+    the march's own load stream replayed without arithmetic on the same
+    views (nes_probe_gather_replay, L2 flushed before each replay, median),
+    and the random-gather rates of 4-, 16- and 32-byte loads over an
+    L2-resident 32 MiB table (nes_probe_gather, CUDA events, median of
+    `reps` launches)."""
+    import ctypes
+    import torch
+    import nes
+    lib = nes.load()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sink = torch.empty(max(sms * 512, sms * 2048), dtype=torch.int32, device=dev)
+    arr = (nes.NesView * len(views))(*views)
+    ms = ctypes.c_float(0)
+    rep = []
+    for i in range(reps + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        nes.check(lib.nes_probe_gather_replay(r.h, arr, len(views), sink.data_ptr(), sink.numel(), ctypes.byref(ms)),
+                  "nes_probe_gather_replay")
+        if i:
+            rep.append(ms.value)
+    out = {"replay_ms": round(statistics.median(rep), 3)}
+    table = torch.randint(0, 1 << 30, ((32 << 20) // 4,), dtype=torch.int32, device=dev)
+    threads, loads = sms * 2048, 256
+    for nbytes in (4, 16, 32):
+        t = []
+        for i in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            nes.check(lib.nes_probe_gather(table.data_ptr(), table.numel() * 4, nbytes, loads, threads,
+                                           sink.data_ptr(), ctypes.c_void_p(stream.cuda_stream)), "nes_probe_gather")
+            b.record(stream)
+            b.synchronize()
+            if i:
+                t.append(a.elapsed_time(b))
+        sec = statistics.median(t) / 1e3
+        out["random_%dB" % nbytes] = {"gbs": round(threads * loads * nbytes / sec / 1e9, 1),
+                                      "gloads_per_s": round(threads * loads / sec / 1e9, 2)}
+    out["random_note"] = ("uniformly random loads over a 32 MiB L2-resident table, %d threads x %d loads, "
+                          "no locality: the hardware's gather rate" % (threads, loads))
+    return out
 
 
 def cpu_baseline_with_parity(dev, pose, npx):
@@ -401,15 +496,33 @@ def cpu_baseline_with_parity(dev, pose, npx):
                                "against": "FP64 oracle"}}
 
 
-def run_stereo(dev, steps):
-    """Precision-form workload: stereo 2x1920x1832 per request, 100 deg FOV,
-    IPD 0.063, poses on the r = 1.2..2.0 shell; per-request device time of
-    raygen + march + RGB24 + YUV420P + depth packing for both eyes."""
+def _pct(vals, q):
+    v = sorted(vals)
+    return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))]
+
+
+def run_stereo(dev, nposes=200, parity_px=512, sweep_poses=20, log2_tables=(14, 19, 22)):
+    """Precision form: stereo 2x1920x1832 per request (100 deg FOV, IPD
+    0.063), nposes poses on the r = 1.2..2.0 shell, FP16 tcgen05, T = 2^19.
+
+      device  CUDA events around raygen + march + RGB24 + YUV420P + depth
+              packing of both eyes (pose already on the host);
+      host    pose -> YUV420P + uint16 depth of both eyes in pinned host
+              memory through nes_render_yuv_views (host clock, D2H inside);
+      parity  for EVERY pose, `parity_px` seeded random pixels per eye of
+              the tensor-core render against the FP64 oracle: PSNR and max
+              |depth error| (scene extent 1);
+      sweep   T = 2^14 / 2^19 / 2^22: device Mrays/s over sweep_poses poses
+              and the parity of one pose per table size."""
+    import numpy as np
     import torch
     import nes
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
     SW, SH = 1920, 1832
+    px_eye = SW * SH
     f = nes.focal_from_fov(SW, 100.0)
-    poses = nes.shell_poses(0, 200, 1.2, 2.0)
+    poses = nes.shell_poses(0, nposes, 1.2, 2.0)
     ls = nes.linesizes(SW)
     ch = (SH + 1) // 2
     stream = torch.cuda.current_stream(dev)
@@ -417,40 +530,119 @@ def run_stereo(dev, steps):
     lib = nes.load()
     bufs = []
     for _ in range(2):
-        bufs.append(dict(rgb=torch.empty(SW * SH * 3, device=dev), dep=torch.empty(SW * SH, device=dev),
-                         rgb8=torch.empty(SW * SH * 3, dtype=torch.uint8, device=dev),
+        bufs.append(dict(rgb=torch.empty(px_eye * 3, device=dev), dep=torch.empty(px_eye, device=dev),
+                         rgb8=torch.empty(px_eye * 3, dtype=torch.uint8, device=dev),
                          yuv=torch.empty(ls[0] * SH + 2 * ls[1] * ch, dtype=torch.uint8, device=dev),
-                         dmm=torch.empty(SW * SH, dtype=torch.int16, device=dev)))
-    with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=2 * SW * SH, device=dev.index) as r:
-        def request(i):
-            eyes = nes.stereo_pair(poses[i % len(poses)], 0.063)
-            r.render_views([nes.make_view(m, SW, SH, f) for m in eyes], [b["rgb"].data_ptr() for b in bufs],
-                           [b["dep"].data_ptr() for b in bufs], sptr)
-            for b in bufs:
-                y = b["yuv"].data_ptr()
-                nes.check(lib.nes_rgb_to_rgb24(b["rgb"].data_ptr(), SW * SH * 3, b["rgb8"].data_ptr(), sptr), "rgb24")
-                nes.rgb24_to_yuv420p(b["rgb8"].data_ptr(), SW, SH, SW * 3, y, y + ls[0] * SH,
-                                     y + ls[0] * SH + ls[1] * ch, ls, sptr)
-                nes.depth_pack_u16mm(b["dep"].data_ptr(), SW * SH, b["dmm"].data_ptr(), sptr)
-        for i in range(3):
-            request(i)
-        torch.cuda.synchronize()
+                         dmm=torch.empty(px_eye, dtype=torch.int16, device=dev)))
+    host = [[torch.empty(n, dtype=torch.uint8).pin_memory() for n in (ls[0] * SH, ls[1] * ch, ls[2] * ch)] +
+            [torch.empty(px_eye, dtype=torch.int16).pin_memory()] for _ in range(2)]
+    rng = np.random.default_rng(2024)
+    pix_sets = [[np.sort(rng.choice(px_eye, parity_px, replace=False)).astype(np.int64) for _ in range(2)]
+                for _ in range(nposes)]
+
+    def eyes_of(i, focal=f):
+        return [nes.make_view(m, SW, SH, focal) for m in nes.stereo_pair(poses[i % len(poses)], 0.063)]
+
+    def device_request(r, i):
+        r.render_views(eyes_of(i), [b["rgb"].data_ptr() for b in bufs], [b["dep"].data_ptr() for b in bufs], sptr)
+        for b in bufs:
+            y = b["yuv"].data_ptr()
+            nes.check(lib.nes_rgb_to_rgb24(b["rgb"].data_ptr(), px_eye * 3, b["rgb8"].data_ptr(), sptr), "rgb24")
+            nes.rgb24_to_yuv420p(b["rgb8"].data_ptr(), SW, SH, SW * 3, y, y + ls[0] * SH,
+                                 y + ls[0] * SH + ls[1] * ch, ls, sptr)
+            nes.depth_pack_u16mm(b["dep"].data_ptr(), px_eye, b["dmm"].data_ptr(), sptr)
+
+    def timed_device(r, n, collect=None):
         ms, samples = [], []
-        for i in range(steps):
+        for i in range(n):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            request(i)
+            device_request(r, i)
             b.record(stream)
             b.synchronize()
             ms.append(a.elapsed_time(b))
             samples.append(r.last_sample_count())
-    ms_sorted = sorted(ms)
-    return {"workload": "stereo 2x1920x1832, 100 deg FOV, IPD 0.063, poses on r=1.2..2.0 shell, FP16 tcgen05",
-            "requests": steps, "p50_ms": round(ms_sorted[len(ms) // 2], 3),
-            "p99_ms": round(ms_sorted[min(len(ms) - 1, int(math.ceil(0.99 * len(ms))) - 1)], 3),
-            "mrays": round(2 * SW * SH * steps / (sum(ms) / 1e3) / 1e6, 3),
-            "samples_per_pixel": round(statistics.mean(samples) / (2 * SW * SH), 2),
-            "timing": "CUDA events around each request (device time, pose already on the host)"}
+            if collect is not None:
+                collect(i)
+        return ms, samples
+
+    gpu_px = []  # per pose: (rgb [2, parity_px, 3], depth [2, parity_px]) of the device render
+
+    def grab(i):
+        rr, dd = [], []
+        for e, b in enumerate(bufs):
+            idx = torch.from_numpy(pix_sets[i][e]).to(dev)
+            rr.append(b["rgb"].view(-1, 3).index_select(0, idx).cpu().numpy())
+            dd.append(b["dep"].index_select(0, idx).cpu().numpy())
+        gpu_px.append((rr, dd))
+
+    out = {"workload": "stereo 2x1920x1832 per request, 100 deg FOV, IPD 0.063, %d poses on r=1.2..2.0 shell, "
+                       "FP16 tcgen05, seed 0" % nposes}
+    with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=2 * px_eye, device=dev.index) as r:
+        for i in range(3):
+            device_request(r, i)
+        torch.cuda.synchronize()
+        ms, samples = timed_device(r, nposes, collect=grab)
+        # Pose -> YUV on the host (D2H of both eyes' planes and depth inside).
+        hy, hu, hv, hd = ([h[k].data_ptr() for h in host] for k in range(4))
+        for i in range(3):
+            r.render_yuv_views(eyes_of(i), hy, hu, hv, ls, hd)
+        lat = []
+        for i in range(nposes):
+            t0 = time.perf_counter()
+            r.render_yuv_views(eyes_of(i), hy, hu, hv, ls, hd)
+            lat.append(1e3 * (time.perf_counter() - t0))
+    out["device"] = {"requests": nposes, "p50_ms": round(_pct(ms, 0.5), 3), "p99_ms": round(_pct(ms, 0.99), 3),
+                     "mrays": round(2 * px_eye * nposes / (sum(ms) / 1e3) / 1e6, 3),
+                     "samples_per_pixel": round(statistics.mean(samples) / (2 * px_eye), 2),
+                     "timing": "CUDA events around each request (pose already on the host)"}
+    d2h = 2 * (host[0][0].numel() + host[0][1].numel() + host[0][2].numel() + 2 * host[0][3].numel())
+    out["host_pose_to_yuv"] = {"requests": nposes, "p50_ms": round(_pct(lat, 0.5), 3),
+                               "p99_ms": round(_pct(lat, 0.99), 3),
+                               "mrays": round(2 * px_eye * nposes / (sum(lat) / 1e3) / 1e6, 3),
+                               "d2h_bytes_per_request": d2h,
+                               "timing": "host clock around nes_render_yuv_views (pose on the host -> YUV420P + "
+                                         "uint16 depth of both eyes in pinned host memory)"}
+    # Per-pose parity against the FP64 oracle.
+    scene = oracle.Scene(0, 19)
+    threads = os.cpu_count() or 1
+    psnrs, derr = [], []
+    t0 = time.perf_counter()
+    for i in range(nposes):
+        for e, m in enumerate(nes.stereo_pair(poses[i], 0.063)):
+            o_rgb, o_dep, _ = scene.render(m, SW, SH, f, pixels=pix_sets[i][e].astype(np.int32), nthreads=threads)
+            g_rgb, g_dep = gpu_px[i][0][e], gpu_px[i][1][e]
+            psnrs.append(oracle.psnr(g_rgb, o_rgb))
+            derr.append(float(np.abs(g_dep - o_dep).max()))
+    out["parity"] = {"against": "FP64 oracle", "pixels_per_eye_per_pose": parity_px, "poses": nposes,
+                     "per_pose_min_psnr_db": round(min(psnrs), 2), "median_psnr_db": round(statistics.median(psnrs), 2),
+                     "max_depth_err": max(derr), "all_pass": bool(min(psnrs) >= 45.0 and max(derr) <= 1e-3),
+                     "oracle_seconds": round(time.perf_counter() - t0, 1)}
+    # Table-size sweep.
+    sweep = {}
+    for lg in log2_tables:
+        with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=2 * px_eye, device=dev.index,
+                          log2_table_size=lg) as r:
+            for i in range(2):
+                device_request(r, i)
+            torch.cuda.synchronize()
+            gpu_px.clear()
+            ms_t, samp_t = timed_device(r, sweep_poses, collect=lambda i: grab(i) if i == 0 else None)
+        sc = scene if lg == 19 else oracle.Scene(0, lg)
+        ps, de = [], []
+        for e, m in enumerate(nes.stereo_pair(poses[0], 0.063)):
+            o_rgb, o_dep, _ = sc.render(m, SW, SH, f, pixels=pix_sets[0][e].astype(np.int32), nthreads=threads)
+            ps.append(oracle.psnr(gpu_px[0][0][e], o_rgb))
+            de.append(float(np.abs(gpu_px[0][1][e] - o_dep).max()))
+        sweep["2^%d" % lg] = {"mrays": round(2 * px_eye * sweep_poses / (sum(ms_t) / 1e3) / 1e6, 3),
+                              "p50_ms": round(_pct(ms_t, 0.5), 3), "table_mib_fp16": (16 << lg) * 4 // (1 << 20),
+                              "pose0_min_psnr_db": round(min(ps), 2), "pose0_max_depth_err": max(de)}
+        del sc
+    out["table_sweep"] = sweep
+    out["table_sweep_note"] = ("device Mrays/s over %d poses per table size (2 warm-up requests each); parity of "
+                               "pose 0 (%d pixels per eye) against the FP64 oracle of the same table size"
+                               % (sweep_poses, parity_px))
+    return out
 
 
 def run_glue(dev, peaks):
@@ -549,14 +741,15 @@ def run_glue(dev, peaks):
     return out
 
 
-def run_training(dev, steps, nviews=32, side=400, batch=1 << 18):
-    """Refit workload: an FP32 teacher (seed 1, T=2^19) renders nviews
-    side x side targets from the r = 1.2..2.0 shell; an FP32 student (seed
-    2) takes Adam steps of `batch` rays (lr 1e-2, L2 RGB + 0.1 L2 depth).
-    Each step is synchronous; its device phases come from CUDA events on the
-    trainer's stream and the step time from the host clock around the call.
-    PSNR of the student against the teacher on a held-out view before and
-    after the timed steps."""
+def run_training(dev, steps, nviews=64, side=800, batch=1 << 18, curve_points=16):
+    """Differentiation form: an FP32 teacher (seed 1, T=2^19) renders nviews
+    side x side targets (60 deg FOV) from the r = 1.2..2.0 shell; an FP32
+    student (seed 2) takes Adam steps of `batch` rays sampled uniformly over
+    the views (lr 1e-2, betas (0.9, 0.99), eps 1e-15, L2 RGB + 0.1 L2
+    depth).  Each step is synchronous; its device phases come from CUDA
+    events on the trainer's stream and the step time from the host clock
+    around the call.  PSNR of the student against the teacher on a held-out
+    view before and after the steps."""
     import numpy as np
     import torch
     import nes
@@ -587,25 +780,30 @@ def run_training(dev, steps, nviews=32, side=400, batch=1 << 18):
             tr.set_targets(views, rgb.data_ptr(), dep.data_ptr())
             losses = [tr.step(1000 + i) for i in range(3)]  # warm-up steps (part of the refit)
             wall, phases, samples = [], [], []
+            t_all = time.perf_counter()
             for i in range(steps):
                 t0 = time.perf_counter()
                 losses.append(tr.step(i))
                 wall.append(time.perf_counter() - t0)
                 phases.append(tr.last_timings())
                 samples.append(tr.last_samples())
+            t_all = time.perf_counter() - t_all
         p1 = psnr(student)
     ms = 1e3 * statistics.median(wall)
     fwd, bwd, adam = (statistics.median(p[k] for p in phases) for k in range(3))
-    return {"workload": "refit teacher seed 1 -> student seed 2, T=2^19, %d views %dx%d, %d rays/step, Adam lr 1e-2"
-                        % (nviews, side, side, batch),
-            "steps": steps, "ms_per_step": round(ms, 2), "mrays_per_s": round(batch / ms / 1e3, 3),
+    every = max(1, len(losses) // curve_points)
+    return {"workload": "refit teacher seed 1 -> student seed 2, T=2^19, %d views %dx%d (60 deg FOV, r=1.2..2.0 "
+                        "shell), %d rays/step sampled uniformly over the views, Adam lr 1e-2 betas (0.9, 0.99) "
+                        "eps 1e-15, loss L2 RGB + 0.1 L2 depth" % (nviews, side, side, batch),
+            "steps": steps, "warmup_steps": 3, "ms_per_step": round(ms, 2), "mrays_per_s": round(batch / ms / 1e3, 3),
+            "total_s": round(t_all, 1),
             "samples_per_step": int(statistics.median(samples)),
             "msamples_per_s": round(statistics.median(samples) / ms / 1e3, 1),
             "phase_ms": {"forward": round(fwd, 2), "backward": round(bwd, 2), "adam": round(adam, 2)},
-            "loss": {"first": round(losses[0], 6), "last": round(losses[-1], 6),
-                     "curve": [round(v, 6) for v in losses[::max(1, len(losses) // 8)]]},
+            "loss": {"first": round(losses[0], 7), "last": round(losses[-1], 7),
+                     "curve_every": every, "curve": [round(v, 7) for v in losses[::every]]},
             "held_out_psnr_db": {"before": p0, "after": p1},
-            "timing": "host clock around each synchronous step; phases from CUDA events"}
+            "timing": "host clock around each synchronous step (median); phases from CUDA events (median)"}
 
 
 def random_walk_poses(seed, n, rmin=1.2, rmax=2.0, jitter_deg=0.5):
@@ -644,6 +842,10 @@ def run_serving(dev, seconds, max_queue_ms=0.0):
     with nes.Renderer(precision=nes.PREC_FP16_TC, max_pixels=2 * 1920 * 1832, device=dev.index) as r:
         srv = nes.Server(r, max_inflight_batches=2, max_batch_pixels=2 * 1920 * 1832,
                          hbm_budget_bytes=80 << 30, max_pending=16, max_queue_ms=max_queue_ms)
+        import torch
+        st0 = srv.stats()
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(dev)[0]
         try:
             # An untimed second at the lowest rate first: graphs for the common
             # batch shapes, the output pool and the throughput estimate settle.
@@ -708,17 +910,22 @@ def run_serving(dev, seconds, max_queue_ms=0.0):
                                   if ls else None,
                                   "mrays": round(pix[0] / wall / 1e6, 3)}
             st = srv.stats()
+            free1 = torch.cuda.mem_get_info(dev)[0]
         finally:
             srv.close()
     out["workload"] = ("Poisson arrivals for %.1f s per rate after 1 s untimed at 90 req/s; mono 640x360 / "
                        "1280x720 / 1920x1080 and stereo "
                        "2x1920x1832 uniformly; random-walk poses on the r=1.2..2.0 shell (0.5 deg jitter); "
-                       "FP16 tcgen05; 2 batches in flight; latency = submit -> YUV+depth on device; admission: "
+                       "FP16 tcgen05; 2 batches in flight; latency = submit -> YUV+depth ready on the device; admission: "
                        "80 GB budget, 16 pending, %s" % (seconds, "expected delay <= %g ms" % max_queue_ms
                                                           if max_queue_ms else "no delay bound"))
     out["batches"] = st["batches"]
-    out["graph_instantiations"] = st["graph_instantiations"]
+    out["graph_instantiations"] = {"at_creation": st0["graph_instantiations"],
+                                   "while_serving": st["graph_instantiations"] - st0["graph_instantiations"]}
     out["graph_updates"] = st["graph_updates"]
+    out["device_free_bytes_change_while_serving"] = int(free1 - free0)
+    out["allocation_note"] = ("outputs are carved from the output arena reserved at server creation; one graph "
+                              "per slot, instantiated at creation, replays every batch shape")
     return out
 
 

@@ -460,6 +460,23 @@ int nes_last_sample_count(nes_ctx *ctx, uint64_t *samples);
  * context stays usable either way.  Blocks until done. */
 int nes_selftest_bounded_wait(nes_ctx *ctx, uint32_t poll_limit, int arrive);
 
+/* Measured ceilings of the tensor-core march's gather stream (the roofline
+ * term next to the MLP's tensor-core term; no counterpart in the reference,
+ * whose renderer is external).  nes_probe_gather queues `threads` threads (a
+ * multiple of 256) that each make loads_per_thread uniformly random loads of
+ * load_bytes (4, 16, or 32 read as two 16-byte loads) over table_bytes of
+ * device memory (table_bytes / load_bytes a power of two), XOR-folded into
+ * sink_dev[thread]; the caller times it on `stream`.
+ * nes_probe_gather_replay replays the march's own load stream for the views
+ * on a tensor-core context -- the same rays, warp refills, sample positions,
+ * record and table addresses, with no interpolation, MLP or compositing --
+ * and returns its device time (CUDA events) in *replay_ms; sink_dev holds at
+ * least (SM count) x 512 words.  Both write nothing but the sink. */
+int nes_probe_gather(const void *table_dev, uint64_t table_bytes, int load_bytes, uint32_t loads_per_thread,
+                     uint32_t threads, uint32_t *sink_dev, void *stream);
+int nes_probe_gather_replay(nes_ctx *ctx, const nes_view *views, int nviews, uint32_t *sink_dev, size_t sink_words,
+                            float *replay_ms);
+
 /* Per-kernel timing with CUDA events recorded on the stream the kernels
  * run on (the reference's ScopedTimer averages, src/server.cpp:172-190,
  * in device time).  When enabled, every render records events around ray

@@ -573,6 +573,47 @@ int nes_selftest_bounded_wait(nes_ctx* c, uint32_t poll_limit, int arrive) {
   return err ? NES_ETIMEDOUT : NES_OK;
 }
 
+int nes_probe_gather(const void* table_dev, uint64_t table_bytes, int load_bytes, uint32_t loads_per_thread,
+                     uint32_t threads, uint32_t* sink_dev, void* stream) {
+  if (!table_dev || !sink_dev || loads_per_thread == 0) return NES_EINVAL;
+  const cudaError_t e = launch_gather_probe(table_dev, table_bytes, load_bytes, loads_per_thread, sink_dev, threads,
+                                            reinterpret_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? NES_OK : (e == cudaErrorInvalidValue ? NES_EINVAL : NES_EIO);
+}
+
+int nes_probe_gather_replay(nes_ctx* c, const nes_view* views, int nviews, uint32_t* sink_dev, size_t sink_words,
+                            float* replay_ms) {
+  if (!c || !views || !sink_dev || !replay_ms) return NES_EINVAL;
+  if (c->cfg.precision != NES_PREC_FP16_TC) return NES_EINVAL;
+  if (sink_words < (size_t)c->num_sms * 512) return NES_EINVAL;
+  std::lock_guard<std::mutex> lock(c->mu);
+  NES_CUDA(cudaSetDevice(c->cfg.device));
+  ViewBatch vb;
+  uint64_t pixels = 0;
+  float* none[kMaxViews] = {};
+  const int rc = fill_view_batch(views, nviews, none, none, c->cfg.max_pixels, &vb, &pixels);
+  if (rc != NES_OK) return rc;
+  NES_CUDA(cudaStreamSynchronize(c->stream));
+  const int prev = collect_status(c);
+  if (prev != NES_OK) return prev;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  NES_CUDA(cudaEventCreate(&ev[0]));
+  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return NES_EIO;
+  }
+  cudaError_t e = cudaMemsetAsync(c->scratch.counters, 0, kCtrWords * sizeof(uint32_t), c->stream);
+  if (e == cudaSuccess) e = launch_raygen(vb, c->scratch, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[0], c->stream);
+  if (e == cudaSuccess) e = launch_gather_replay(vb, c->scene, c->scratch, c->num_sms, sink_dev, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(replay_ms, ev[0], ev[1]);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  return e == cudaSuccess ? NES_OK : NES_EIO;
+}
+
 int nes_set_profiling(nes_ctx* c, int enable) {
   if (!c) return NES_EINVAL;
   std::lock_guard<std::mutex> lock(c->mu);

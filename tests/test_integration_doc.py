@@ -42,6 +42,8 @@ extern nesproto::Camera cam;
 extern uint32_t w, h;
 extern float fov_deg;
 extern AVFrame* avframe;
+extern AVFrame *left, *right;
+extern uint16_t *left_depth_mm, *right_depth_mm;
 extern uint16_t* depth_mm;
 extern nes_ctx* nes;
 extern nes_view left_view, right_view;

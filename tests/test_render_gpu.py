@@ -102,18 +102,44 @@ def test_stereo_pair_vs_oracle(renderer, cuda, scene0, nes_lib):
         assert np.abs(dep - odep).max() <= DEPTH_TOL
 
 
-def test_stereo_1832_pixel_subset_vs_oracle(rtc, cuda, scene0, nes_lib):
-    """The precision-form workload: a stereo pair of 1920x1832 views at
-    100 deg FOV from the r = 1.2..2.0 shell, IPD 0.063, on the tensor cores."""
-    pose = nes_lib.shell_poses(0, 200, 1.2, 2.0)[11]
+@pytest.mark.parametrize("k", [11, 57, 103, 149, 199])
+def test_stereo_1832_pixel_subset_vs_oracle(rtc, cuda, scene0, nes_lib, k):
+    """The precision-form workload: stereo pairs of 1920x1832 views at
+    100 deg FOV from the r = 1.2..2.0 shell, IPD 0.063, on the tensor cores;
+    poses spread over the 200-pose set, each eye against the FP64 oracle on
+    a seeded pixel subset, with the frame's sample count exact."""
+    pose = nes_lib.shell_poses(0, 200, 1.2, 2.0)[k]
     W, H = 1920, 1832
     f = nes_lib.focal_from_fov(W, 100.0)
     views = [(m, W, H, f) for m in nes_lib.stereo_pair(pose, 0.063)]
     out = render_gpu(rtc, cuda, views)
-    rng = np.random.default_rng(8)
+    rng = np.random.default_rng(8 + k)
     for (M, _, _, _), (rgb, dep) in zip(views, out):
-        pix = rng.choice(W * H, 2000, replace=False).astype(np.int32)
+        pix = rng.choice(W * H, 1500, replace=False).astype(np.int32)
         orgb, odep, _ = scene0.render(M, W, H, f, pixels=pix)
+        assert psnr(rgb[pix], orgb) >= PSNR_MIN
+        assert np.abs(dep[pix] - odep).max() <= DEPTH_TOL
+
+
+@pytest.mark.parametrize("log2T", [14, 22])
+def test_table_sweep_stereo_1832_vs_oracle(nes_lib, oracle_mod, cuda, log2T):
+    """The table sweep at the precision form's full size: one stereo
+    2x1920x1832 request per table size on the tensor cores, each eye against
+    the FP64 oracle of the same table size on a seeded pixel subset."""
+    scene = oracle_mod.Scene(0, log2T)
+    pose = nes_lib.shell_poses(0, 200, 1.2, 2.0)[31]
+    W, H = 1920, 1832
+    f = nes_lib.focal_from_fov(W, 100.0)
+    views = [(m, W, H, f) for m in nes_lib.stereo_pair(pose, 0.063)]
+    r = nes_lib.Renderer(precision=nes_lib.PREC_FP16_TC, log2_table_size=log2T, max_pixels=2 * W * H)
+    try:
+        out = render_gpu(r, cuda, views)
+    finally:
+        r.close()
+    rng = np.random.default_rng(log2T)
+    for (M, _, _, _), (rgb, dep) in zip(views, out):
+        pix = rng.choice(W * H, 1000, replace=False).astype(np.int32)
+        orgb, odep, _ = scene.render(M, W, H, f, pixels=pix)
         assert psnr(rgb[pix], orgb) >= PSNR_MIN
         assert np.abs(dep[pix] - odep).max() <= DEPTH_TOL
 
