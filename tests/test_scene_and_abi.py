@@ -187,3 +187,25 @@ def test_linesizes(nes_lib):
     assert nes_lib.linesizes(1280) == [1280, 640, 640]
     assert nes_lib.linesizes(1920) == [1920, 960, 960]
     assert nes_lib.linesizes(33) == [64, 32, 32]
+
+
+def test_probe_and_selftest_entries_reject_bad_arguments_without_gpu(nes_lib):
+    """The gather probes, the bounded-wait self-test and the multi-view
+    pose->YUV call check their arguments before any CUDA call."""
+    lib = nes_lib.load()
+    sink = ctypes.c_void_p(0x1000)
+    table = ctypes.c_void_p(0x2000)
+    EINVAL = nes_lib.NES_EINVAL
+    assert lib.nes_probe_gather(None, 1 << 25, 4, 16, 256, sink, None) == EINVAL
+    assert lib.nes_probe_gather(table, 1 << 25, 4, 16, 256, None, None) == EINVAL
+    assert lib.nes_probe_gather(table, 1 << 25, 4, 0, 256, sink, None) == EINVAL
+    assert lib.nes_probe_gather(table, 1 << 25, 8, 16, 256, sink, None) == EINVAL      # 4, 16 or 32 bytes
+    assert lib.nes_probe_gather(table, 3 << 20, 4, 16, 256, sink, None) == EINVAL      # not a power of two
+    assert lib.nes_probe_gather(table, 1 << 25, 16, 16, 100, sink, None) == EINVAL     # threads % 256
+    ms = ctypes.c_float(0)
+    assert lib.nes_probe_gather_replay(None, None, 1, sink, 1 << 20, ctypes.byref(ms)) == EINVAL
+    assert lib.nes_selftest_bounded_wait(None, 100, 0) == EINVAL
+    ls = (ctypes.c_int * 3)(64, 32, 32)
+    views = (nes_lib.NesView * 2)()
+    ptrs = (ctypes.c_void_p * 2)(0x1000, 0x2000)
+    assert lib.nes_render_yuv_views(None, views, 2, ptrs, ptrs, ptrs, ls, None) == EINVAL
