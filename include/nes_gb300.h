@@ -322,6 +322,13 @@ int nes_trainer_grad(nes_trainer *tr, const int32_t *rays, int n, double *loss, 
 int nes_trainer_loss_fp64(nes_trainer *tr, const int32_t *rays, int n, int which, uint64_t index, double delta,
                           double *loss);
 
+/* The same FP64 loss for m perturbations in one launch (1..65535):
+ * perturbation j adds delta[j] to entry index[j] of array which[j] (0 table,
+ * 1 weights blob); losses[j] receives its loss.  For checking many
+ * parameters by central differences at once. */
+int nes_trainer_loss_fp64_batch(nes_trainer *tr, const int32_t *rays, int n, int m, const int32_t *which,
+                                const uint64_t *index, const double *delta, double *losses);
+
 /* Samples evaluated (and backpropagated) by the last loss/gradient pass. */
 uint64_t nes_trainer_last_samples(const nes_trainer *tr);
 

@@ -1185,6 +1185,47 @@ __global__ void loss_f64_kernel(const TrainRay* __restrict__ rays, int n, const 
   atomicAdd(loss_sum, (e0 * e0 + e1 * e1 + e2 * e2 + depth_w * ed * ed) * inv_n);
 }
 
+// The same loss for m perturbations at once (blockIdx.y = perturbation):
+// a central-difference check of many parameters in one launch instead of one
+// launch per evaluation (each evaluation alone fills one or two SMs).
+struct PerturbF64 {
+  int which;
+  uint64_t index;
+  double delta;
+};
+
+__global__ void loss_f64_batch_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, const float* table,
+                                      const float* w, const PerturbF64* __restrict__ pert,
+                                      double* __restrict__ loss_sums, double depth_w, double inv_n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PerturbF64 q = pert[blockIdx.y];
+  ParamsF64 P;
+  P.table = table;
+  P.w = w;
+  P.which = q.which;
+  P.index = q.index;
+  P.delta = q.delta;
+  const TrainRay r = rays[i];
+  double C[3] = {0, 0, 0}, D = 0, T = 1;
+  const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
+  for (int s = 0; s < r.n; ++s) {
+    const float t = fmaf((float)s + 0.5f, kDt, r.ts);
+    const float3 x = sample_pos(o, d, t);
+    if (!occupied(sc.occ, x)) continue;
+    double sigma, c[3];
+    query_f64(P, sc, x, d, sigma, c);
+    const double alpha = -expm1(-sigma * (double)kDt);
+    const double wgt = T * alpha;
+    for (int a = 0; a < 3; ++a) C[a] += wgt * c[a];
+    D += wgt * (double)t;
+    T -= wgt;
+    if (T < (double)kTStop) break;
+  }
+  const double e0 = C[0] - r.tr, e1 = C[1] - r.tg, e2 = C[2] - r.tb, ed = D - r.td;
+  atomicAdd(loss_sums + blockIdx.y, (e0 * e0 + e1 * e1 + e2 * e2 + depth_w * ed * ed) * inv_n);
+}
+
 }  // namespace
 
 struct nes_trainer {
@@ -1568,6 +1609,45 @@ int nes_trainer_loss_fp64(nes_trainer* t, const int32_t* rays, int n, int which,
   TR_CUDA(cudaMemcpyAsync(&err, t->d_ctr + 1, sizeof(err), cudaMemcpyDeviceToHost, t->st));
   TR_CUDA(cudaMemcpyAsync(loss, t->d_loss, sizeof(double), cudaMemcpyDeviceToHost, t->st));
   TR_CUDA(cudaStreamSynchronize(t->st));
+  return err ? NES_EINVAL : NES_OK;
+}
+
+int nes_trainer_loss_fp64_batch(nes_trainer* t, const int32_t* rays, int n, int m, const int32_t* which,
+                                const uint64_t* index, const double* delta, double* losses) {
+  if (!t || !which || !index || !delta || !losses || m < 1 || m > 65535) return NES_EINVAL;
+  const uint64_t limits[2] = {(uint64_t)kLevels * t->ctx->scene.T * 2, (uint64_t)kWeightFloats};
+  std::vector<PerturbF64> host((size_t)m);
+  for (int j = 0; j < m; ++j) {
+    if (which[j] != 0 && which[j] != 1) return NES_EINVAL;
+    if (index[j] >= limits[which[j]]) return NES_EINVAL;
+    host[j] = PerturbF64{which[j], index[j], delta[j]};
+  }
+  std::lock_guard<std::mutex> lk(t->ctx->mu);  // no render of the context meanwhile
+  TR_CUDA(cudaSetDevice(t->ctx->cfg.device));
+  int rc = upload_rays(t, rays, n);
+  if (rc != NES_OK) return rc;
+  PerturbF64* d_pert = nullptr;
+  double* d_loss = nullptr;
+  if (cudaMalloc(&d_pert, sizeof(PerturbF64) * (size_t)m) != cudaSuccess) return NES_ENOMEM;
+  if (cudaMalloc(&d_loss, sizeof(double) * (size_t)m) != cudaSuccess) {
+    cudaFree(d_pert);
+    return NES_ENOMEM;
+  }
+  cudaError_t e = cudaMemcpyAsync(d_pert, host.data(), sizeof(PerturbF64) * (size_t)m, cudaMemcpyHostToDevice, t->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_loss, 0, sizeof(double) * (size_t)m, t->st);
+  if (e == cudaSuccess) {
+    loss_f64_batch_kernel<<<dim3((n + 63) / 64, m), 64, 0, t->st>>>(
+        t->d_rays, n, t->ctx->scene, reinterpret_cast<const float*>(t->ctx->d_table32), t->ctx->d_weights, d_pert,
+        d_loss, (double)t->cfg.depth_weight, 1.0 / (double)n);
+    e = cudaGetLastError();
+  }
+  uint32_t err = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err, t->d_ctr + 1, sizeof(err), cudaMemcpyDeviceToHost, t->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(losses, d_loss, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, t->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(t->st);
+  cudaFree(d_pert);
+  cudaFree(d_loss);
+  if (e != cudaSuccess) return NES_EIO;
   return err ? NES_EINVAL : NES_OK;
 }
 

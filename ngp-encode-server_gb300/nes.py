@@ -155,6 +155,7 @@ _SIGS = {
     "nes_trainer_grad": (_I, [_P, _P, _I, ctypes.POINTER(ctypes.c_double), _P, _P]),
     "nes_trainer_loss_fp64": (_I, [_P, _P, _I, _I, ctypes.c_uint64, ctypes.c_double,
                                    ctypes.POINTER(ctypes.c_double)]),
+    "nes_trainer_loss_fp64_batch": (_I, [_P, _P, _I, _I, _P, _P, _P, _P]),
     "nes_trainer_last_samples": (ctypes.c_uint64, [_P]),
     "nes_trainer_last_timings": (_I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                       ctypes.POINTER(ctypes.c_float)]),
@@ -399,6 +400,19 @@ class Trainer:
         check(self.lib.nes_trainer_loss_fp64(self.h, p.ctypes.data, len(p), which, index, delta,
                                              ctypes.byref(loss)), "nes_trainer_loss_fp64")
         return loss.value
+
+    def loss_fp64_batch(self, pairs, which, index, delta):
+        """FP64 loss for many single-parameter perturbations in one launch."""
+        import numpy as np
+        p = self._pairs(pairs)
+        w = np.ascontiguousarray(which, dtype=np.int32)
+        i = np.ascontiguousarray(index, dtype=np.uint64)
+        d = np.ascontiguousarray(delta, dtype=np.float64)
+        out = np.empty(len(w), np.float64)
+        check(self.lib.nes_trainer_loss_fp64_batch(self.h, p.ctypes.data, len(p), len(w), w.ctypes.data,
+                                                   i.ctypes.data, d.ctypes.data, out.ctypes.data),
+              "nes_trainer_loss_fp64_batch")
+        return out
 
     def last_samples(self):
         return self.lib.nes_trainer_last_samples(self.h)

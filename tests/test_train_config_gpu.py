@@ -156,22 +156,27 @@ def test_gradient_vs_oracle_64_rays(nes_lib, oracle_mod, teacher, cuda, exact):
 
 def test_finite_differences_1024_params(nes_lib, oracle_mod, teacher):
     """Central FP64 differences with h = 1e-4 on 1,024 seeded random
-    parameters.  A parameter whose loss has a kink inside [-h, h] (a ReLU
-    pre-activation or a cell boundary crossing zero there) has no derivative
-    for the difference to match: such a parameter is recognised by its two
-    one-sided differences disagreeing, and at most 1 % of the checks may be
-    kinks."""
+    parameters, on 64 rays.  Each check allows 1e-3 of the gradient plus
+    2e-4 of the largest gradient in the parameter's block (weight block or
+    table level): the FP32 gradient is a sum of tens of thousands of
+    per-sample terms of both signs, so a small entry carries the block's
+    absolute rounding error.  A parameter whose loss has a kink inside
+    [-h, h] (a ReLU pre-activation or a cell boundary crossing zero there)
+    has no derivative for the difference to match: such a parameter is
+    recognised by its two one-sided differences disagreeing, and at most 1 %
+    of the checks may be kinks."""
     views, rgb, dep = teacher
     r, t = _student(nes_lib, teacher, exact_weight_grads=1)
     try:
-        pairs = _pairs(128, 4)
+        pairs = _pairs(64, 4)
         loss, gt, gw = t.grad(pairs, TABLE_FLOATS)
         l0 = t.loss_fp64(pairs)
         assert abs(l0 - loss) <= 1e-5 * l0
         rng = np.random.default_rng(1024)
         checks = []
         for a, b in BLOCKS.values():
-            checks += [(1, int(i), float(gw[i])) for i in rng.choice(np.arange(a, b), 100, replace=False)]
+            scale = float(np.abs(gw[a:b]).max())
+            checks += [(1, int(i), float(gw[i]), scale) for i in rng.choice(np.arange(a, b), 100, replace=False)]
         touched = np.flatnonzero(gt)
         per_level = []
         for lvl in range(16):
@@ -187,23 +192,33 @@ def test_finite_differences_1024_params(nes_lib, oracle_mod, teacher):
                 i = int(rng.integers(lo, lo + T * 2))
                 if gt[i] == 0.0 and i not in pick:
                     pick.append(i)
-            checks += [(0, int(i), float(gt[i])) for i in pick]
+            scale = float(np.abs(gt[lo:lo + T * 2]).max())
+            checks += [(0, int(i), float(gt[i]), scale) for i in pick]
         assert len(checks) == 1024
         h = 1e-4
+        # Every +h and -h evaluation in one launch (one block of rays each).
+        wh = [c[0] for c in checks] * 2
+        ix = [c[1] for c in checks] * 2
+        dl = [h] * len(checks) + [-h] * len(checks)
+        ls = t.loss_fp64_batch(pairs, wh, ix, dl)
+        # The batched form agrees with single evaluations.
+        for j in (0, 517, 1023):
+            assert ls[j] == pytest.approx(t.loss_fp64(pairs, checks[j][0], checks[j][1], h), rel=1e-12)
         fails, kinks = [], []
-        for which, idx, g in checks:
-            lp = t.loss_fp64(pairs, which, idx, h)
-            lm = t.loss_fp64(pairs, which, idx, -h)
+        worst = 0.0
+        for j, (which, idx, g, scale) in enumerate(checks):
+            lp, lm = ls[j], ls[len(checks) + j]
             fd = (lp - lm) / (2 * h)
-            tol = 1e-3 * abs(g) + 1e-10
-            if abs(fd - g) <= tol:
-                continue
+            tol = 1e-3 * abs(g) + 2e-4 * scale + 1e-12
             right, left = (lp - l0) / h, (l0 - lm) / h
-            if abs(right - left) > 10 * tol:
+            if abs(fd - g) > tol and abs(right - left) > 10 * tol:
                 kinks.append((which, idx, g, fd, left, right))
-            else:
+                continue
+            worst = max(worst, abs(fd - g) / tol)
+            if abs(fd - g) > tol:
                 fails.append((which, idx, g, fd))
-        print("FD: %d checks, %d kinks, %d failures" % (len(checks), len(kinks), len(fails)))
+        print("FD: %d checks, %d kinks, %d failures, worst error / tolerance %.3f"
+              % (len(checks), len(kinks), len(fails), worst))
         assert not fails, fails[:10]
         assert len(kinks) <= 10, kinks
     finally:
