@@ -197,8 +197,10 @@ typedef struct nes_server_config {
   uint32_t max_pending;          /* admitted requests waiting for a batch */
   int32_t use_graphs;            /* 1: CUDA graph per batch shape, 0: plain launches */
   float max_queue_ms;            /* > 0: reject a request whose estimated pose -> YUV time
-                                  * (its pixels plus every pixel queued or in flight, at the
-                                  * measured pixel throughput) exceeds this; 0: no bound */
+                                  * (its expected samples plus those of every request queued
+                                  * or in flight -- mean march length of a 16 x 16 grid of each
+                                  * view's rays through the unit cube, times its pixels -- at
+                                  * the measured sample throughput) exceeds this; 0: no bound */
 } nes_server_config;
 
 typedef struct nes_request {

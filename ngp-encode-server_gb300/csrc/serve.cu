@@ -27,7 +27,9 @@
 //    publishes its requests with their pose->YUV latency.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -90,6 +92,7 @@ struct Req {
   int status = NES_OK;
   Clock::time_point t_submit, t_done;
   double pred_ms = 0.0;  // expected pose -> YUV time at admission (0: no estimate yet)
+  double work = 0.0;     // expected cost (samples + pixels), see estimate_work
   uint64_t batch_id = 0;
   uint32_t batch_requests = 0, batch_views = 0;
 };
@@ -115,8 +118,47 @@ struct Slot {
   uint64_t batch_id = 0;
   std::vector<uint64_t> tickets;
   uint64_t pixels = 0;
+  double work = 0.0;
   Clock::time_point t_launch;
 };
+
+// Expected cost of a view in samples: the mean march length (chord through
+// the unit cube / dt, at most the step limit) of a 16 x 16 grid of its rays,
+// times its pixels, plus one per pixel for its ray generation and frame
+// output.  Costs differ by more than 2x between poses of the serving mix
+// (near poses fill the frame with long chords), so the delay bound
+// predicts with this rather than with pixel counts.
+double estimate_work(const nes_view& v) {
+  constexpr int kGrid = 16;
+  const float* M = v.matrix;
+  double steps = 0.0;
+  for (int gy = 0; gy < kGrid; ++gy) {
+    for (int gx = 0; gx < kGrid; ++gx) {
+      const double px = ((double)gx + 0.5) * v.width / kGrid, py = ((double)gy + 0.5) * v.height / kGrid;
+      const double u = (px - 0.5 * v.width) / v.focal_px, w = (py - 0.5 * v.height) / v.focal_px;
+      double d[3], nrm = 0.0;
+      for (int a = 0; a < 3; ++a) {
+        d[a] = M[a * 4 + 0] * u + M[a * 4 + 1] * w + M[a * 4 + 2];
+        nrm += d[a] * d[a];
+      }
+      nrm = std::sqrt(nrm);
+      double tn = -1e30, tf = 1e30;
+      for (int a = 0; a < 3; ++a) {
+        const double da = d[a] / nrm, oa = M[a * 4 + 3];
+        if (std::fabs(da) < 1e-12) {  // parallel to this slab: inside it or a miss
+          if (oa < 0.0 || oa > 1.0) tf = -1e30;
+          continue;
+        }
+        const double t0 = (0.0 - oa) / da, t1 = (1.0 - oa) / da;
+        tn = std::max(tn, std::min(t0, t1));
+        tf = std::min(tf, std::max(t0, t1));
+      }
+      const double ts = std::max(tn, 0.0);
+      if (nrm > 0.0 && tf > ts) steps += std::min((double)kMaxSteps, std::floor((tf - ts) / (double)kDt));
+    }
+  }
+  return ((double)v.width * v.height) * (steps / (kGrid * kGrid) + 1.0);
+}
 
 // First-fit free list over one device allocation: request outputs are
 // carved out at admission and handed back at release, so serving never
@@ -175,14 +217,16 @@ struct nes_server {
   std::deque<uint64_t> pending;
   std::deque<int> launch_order;  // slots in launch order (completion order)
   uint64_t next_ticket = 1, next_batch = 1;
-  // Admission by expected delay: pixels admitted but not yet batched, pixels
-  // of the batches on the GPU, and the measured service rate (pixels per ms,
-  // an exponential average over completed batches; 0 until the first).  The
-  // model leaves out host work between batches (graph updates, allocation)
-  // and batching granularity, so its predictions are scaled by the running
-  // ratio of measured to predicted latency of completed requests.
+  // Admission by expected delay: the expected cost (estimate_work) of the
+  // requests admitted but not yet batched and of the batches on the GPU, and
+  // the measured service rate (cost per ms, an exponential average over
+  // completed batches; 0 until the first).  The model leaves out batching
+  // granularity and host work between batches, so its predictions are
+  // scaled by the running ratio of measured to predicted latency of
+  // completed requests.  Pixel counts still bound the first batch.
   uint64_t pending_pixels = 0, inflight_pixels = 0;
-  double rate_px_per_ms = 0.0, delay_scale = 1.0;
+  double pending_work = 0.0, inflight_work = 0.0;
+  double rate_work_per_ms = 0.0, delay_scale = 1.0;
   Clock::time_point last_done;
   bool stop = false;
   nes_server_stats stats{};
@@ -290,6 +334,7 @@ void scheduler_main(nes_server* s) {
     uint8_t* outs[kMaxViews];
     int nv = 0;
     uint64_t pixels = 0;
+    double work = 0.0;
     while (!s->pending.empty()) {
       Req& r = s->reqs[s->pending.front()];
       uint64_t px = 0;
@@ -301,12 +346,15 @@ void scheduler_main(nes_server* s) {
         outs[nv] = r.dev;
       }
       pixels += px;
+      work += r.work;
       tickets.push_back(s->pending.front());
       batch.push_back(&r);
       s->pending.pop_front();
       s->pending_pixels -= px;
+      s->pending_work -= r.work;
     }
     s->inflight_pixels += pixels;
+    s->inflight_work += work;
     const uint64_t bid = s->next_batch++;
     for (Req* r : batch) {
       r->state = ReqState::Running;
@@ -318,6 +366,7 @@ void scheduler_main(nes_server* s) {
     sl.batch_id = bid;
     sl.tickets = tickets;
     sl.pixels = pixels;
+    sl.work = work;
     sl.t_launch = Clock::now();
     lk.unlock();
 
@@ -333,6 +382,7 @@ void scheduler_main(nes_server* s) {
     s->stats.batches++;
     if (rc != NES_OK) {  // publish the failure; the slot's stream is idle
       s->inflight_pixels -= sl.pixels;
+      s->inflight_work -= sl.work;
       for (uint64_t t : tickets) {
         Req& r = s->reqs[t];
         r.state = ReqState::Done;
@@ -367,13 +417,14 @@ void completion_main(nes_server* s) {
     s->stats.samples += (uint64_t)sl.h_counters[kCtrSamples] | ((uint64_t)sl.h_counters[kCtrSamples + 1] << 32);
     s->stats.pixels += sl.pixels;
     s->inflight_pixels -= sl.pixels;
+    s->inflight_work -= sl.work;
     {  // this batch's service time: from its launch, or from the previous
        // completion if the GPU was still busy with that one
       const Clock::time_point from = sl.t_launch > s->last_done ? sl.t_launch : s->last_done;
       const double ms = std::chrono::duration<double, std::milli>(now - from).count();
-      if (status == NES_OK && ms > 0.0 && sl.pixels) {
-        const double r = (double)sl.pixels / ms;
-        s->rate_px_per_ms = s->rate_px_per_ms > 0.0 ? 0.8 * s->rate_px_per_ms + 0.2 * r : r;
+      if (status == NES_OK && ms > 0.0 && sl.work > 0.0) {
+        const double r = sl.work / ms;
+        s->rate_work_per_ms = s->rate_work_per_ms > 0.0 ? 0.8 * s->rate_work_per_ms + 0.2 * r : r;
       }
       s->last_done = now;
     }
@@ -563,15 +614,16 @@ int nes_submit(nes_server* s, const nes_request* req, uint64_t* ticket) {
     px += (uint64_t)w.width * w.height;
   }
   if (px > s->cfg.max_batch_pixels) return NES_EINVAL;
+  for (uint32_t v = 0; v < req->nviews; ++v) r.work += estimate_work(req->views[v]);
   std::lock_guard<std::mutex> lk(s->mu);
   if (s->stop) return NES_EINVAL;
-  const double pred = s->rate_px_per_ms > 0.0
-                          ? (double)(s->pending_pixels + s->inflight_pixels + px) / s->rate_px_per_ms
+  const double pred = s->rate_work_per_ms > 0.0
+                          ? (s->pending_work + s->inflight_work + r.work) / s->rate_work_per_ms
                           : 0.0;
   // Before the first batch has completed there is no rate: keep at most one
   // batch's worth of pixels in the system.
   const bool late = s->cfg.max_queue_ms > 0.0f &&
-                    (s->rate_px_per_ms > 0.0 ? pred * s->delay_scale > s->cfg.max_queue_ms
+                    (s->rate_work_per_ms > 0.0 ? pred * s->delay_scale > s->cfg.max_queue_ms
                                              : s->pending_pixels + s->inflight_pixels + px > s->cfg.max_batch_pixels);
   size_t off = Arena::kNone;
   if (s->pending.size() < s->cfg.max_pending && !late &&
@@ -584,6 +636,7 @@ int nes_submit(nes_server* s, const nes_request* req, uint64_t* ticket) {
   r.arena_off = off;
   r.dev = s->arena_base + off;
   s->pending_pixels += px;
+  s->pending_work += r.work;
   s->stats.submitted++;
   s->stats.budget_used_bytes += r.bytes;
   r.t_submit = Clock::now();
