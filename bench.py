@@ -52,6 +52,7 @@ DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full 1920x1
 L1_WAVEFRONT_FRAC = {"fp16": 0.694}
 WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
 L2_RULE = "flushed (256 MiB write) before every timed GPU step"
+REC_GB = {10: 1.30, 13: 24.05}  # per-cell corner records of a tensor-core context (32 B per cell)
 
 
 def bench_config():
@@ -75,6 +76,8 @@ def parse_args():
     p.add_argument("--train-batch", type=int, default=1 << 18, help="rays per refit step")
     p.add_argument("--section", choices=["all", "training"], default="all",
                    help="'training' prints only the refit section (for profiling captures)")
+    p.add_argument("--record-levels", type=int, default=13, choices=[10, 13],
+                   help="tensor-core contexts: levels kept as per-cell records (10 only for small profiling captures)")
     p.add_argument("--width", type=int, default=1920, help="smaller sizes only for profiling captures")
     p.add_argument("--height", type=int, default=1080)
     return p.parse_args()
@@ -243,7 +246,7 @@ def run_ours(args):
     results, renderer_used = {}, None
     for prec in precisions:
         try:
-            r = nes.Renderer(precision=prec, max_pixels=W * H, device=local)
+            r = nes.Renderer(precision=prec, max_pixels=W * H, device=local, record_levels=args.record_levels)
         except nes.NesError as e:
             results[prec] = {"error": str(e)}
             continue
@@ -335,8 +338,10 @@ def run_ours(args):
         "ms_per_step": round(head["ms_per_step"], 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": kind, "data": "synthetic (seeded scene and poses)",
         "config": bench_config(),
-        "precision": "FP16 table + FP16 MLP on tcgen05, FP32 accumulate and compositing" if kind == "fp16"
-                     else "FP32 CUDA cores",
+        "precision": "FP16 table + FP16 MLP on tcgen05, FP32 accumulate and compositing; hash-grid levels 0..%d "
+                     "also kept as per-cell corner records (%.1f GB)" % (args.record_levels - 1,
+                                                                         REC_GB[args.record_levels])
+                     if kind == "fp16" else "FP32 CUDA cores",
         "e2e": {"value": round(head["e2e"]["mrays"], 3), "unit": "Mrays/s",
                 "h2d_bytes_per_step": head["e2e"]["h2d"], "d2h_bytes_per_step": head["e2e"]["d2h"],
                 "p50_ms": round(head["e2e"]["p50_ms"], 3), "p99_ms": round(head["e2e"]["p99_ms"], 3)},

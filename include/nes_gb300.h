@@ -65,6 +65,10 @@ typedef struct nes_config {
   float depth_gray_max;      /* scene units mapped to 255 in GRAY8 depth */
   int32_t device;            /* CUDA device ordinal */
   uint32_t max_pixels;       /* largest single-call pixel count (sum over views) */
+  uint32_t record_levels;    /* tensor-core path: hash-grid levels also kept as per-cell records
+                              * of their 8 corner entries (one 32-byte read instead of eight
+                              * scattered gathers): 13 = levels 0..12, 24.0 GB (the default),
+                              * 10 = levels 0..9, 1.30 GB; 0 = the default */
 } nes_config;
 
 /* One view to render: the nes.proto Camera plus a focal length.
@@ -81,7 +85,8 @@ typedef struct nes_view {
   uint32_t flags;  /* reserved, 0 */
 } nes_view;
 
-/* Fills cfg with the reference scene: seed 0, 2^19 entries, FP32, 90 deg. */
+/* Fills cfg with the reference scene: seed 0, 2^19 entries, FP32, 90 deg,
+ * 13 record levels. */
 void nes_config_default(nes_config *cfg);
 
 /* Creates a context on cfg->device: generates the scene, uploads it,

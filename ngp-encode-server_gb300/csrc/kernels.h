@@ -15,12 +15,13 @@ namespace nes {
 struct DevScene {
   const float2* table32 = nullptr;  // [16][T] float2
   const __half2* table16 = nullptr; // [16][T] half2 (tensor-core path)
-  const uint4* rec16 = nullptr;     // per-cell corner records of levels 0..kRecLevels-1 (2 x uint4 each)
+  const uint4* rec16 = nullptr;     // per-cell corner records of levels 0..rec_levels-1 (2 x uint4 each)
   const float* weights = nullptr;   // kWeightFloats FP32 blob
   const uint8_t* tc_weights = nullptr; // FP16 weights in the MMA operand layout
   const uint32_t* occ = nullptr;    // kOccWords
   uint32_t T = 0;
   uint32_t dense_mask = 0;
+  uint32_t rec_levels = 0;          // levels with records (kRecLevelsDefault or kRecLevelsSmall)
 };
 
 // Per-call scratch shared by the render kernels.
@@ -62,8 +63,8 @@ cudaError_t launch_march_tc(const ViewBatch* views_dev, const DevScene& scene, c
 
 // Bytes of the per-cell corner records and their construction from the FP16
 // table (tensor-core path).
-size_t tc_record_bytes();
-cudaError_t launch_build_records(const __half2* table16, uint32_t T, uint32_t dense_mask, uint4* rec,
+size_t tc_record_bytes(int rec_levels);
+cudaError_t launch_build_records(const __half2* table16, uint32_t T, uint32_t dense_mask, int rec_levels, uint4* rec,
                                  cudaStream_t stream);
 
 // Bytes of the FP16 MLP weight image and its packing from the FP32 blob.

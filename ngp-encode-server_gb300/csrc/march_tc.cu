@@ -123,7 +123,7 @@ __device__ __forceinline__ uint32_t interp_lerp(const __half2 (&e)[8], float fx,
 // issue-bound here): integer floor/clamp for the cell, hash terms masked
 // once so each corner index is one 3-input XOR, and the interpolation as
 // packed FP16 lerps (interp_lerp).
-// Levels 0..kRecLevels-1 also exist as per-cell records: the 8 corner
+// The recorded levels (0..kRec-1) also exist as per-cell records: the 8 corner
 // entries of every cell (c = dx + 2 dy + 4 dz) in 32 contiguous bytes, so a
 // sample's level costs two 16-byte loads instead of eight scattered 4-byte
 // gathers (the encoder is bound by L1 wavefronts).  The records are copies of
@@ -182,30 +182,38 @@ __device__ __forceinline__ uint32_t encode_level(const __half2* __restrict__ tab
 // is computed before the first TMEM store: the stores are compiler
 // barriers, so storing per 4 levels would serialise four rounds of
 // gathers per sample.
+template <int L, int kRec>
+__device__ __forceinline__ uint32_t encode_level_any(const __half2* __restrict__ table, const uint4* __restrict__ rec,
+                                                     uint32_t T, uint32_t dense_mask, const float3& x) {
+  if constexpr (L < kRec) return encode_level_rec<L>(rec, x);
+  else return encode_level<L>(table, T, dense_mask, x);
+}
+
+template <int kRec>
 __device__ __forceinline__ void encode_all(const __half2* __restrict__ table, const uint4* __restrict__ rec,
                                            uint32_t T, uint32_t dense_mask, const float3& x, bool has,
                                            uint32_t taddr) {
-  static_assert(kRecLevels == 10, "encode_all reads levels 0..9 from the records");
+  static_assert(kRec >= 10 && kRec <= 13, "records cover levels 0..9 at least, 0..12 at most");
   uint32_t f[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) f[k] = 0u;
   if (has) {
-    f[0] = encode_level_rec<0>(rec, x);
-    f[1] = encode_level_rec<1>(rec, x);
-    f[2] = encode_level_rec<2>(rec, x);
-    f[3] = encode_level_rec<3>(rec, x);
-    f[4] = encode_level_rec<4>(rec, x);
-    f[5] = encode_level_rec<5>(rec, x);
-    f[6] = encode_level_rec<6>(rec, x);
-    f[7] = encode_level_rec<7>(rec, x);
-    f[8] = encode_level_rec<8>(rec, x);
-    f[9] = encode_level_rec<9>(rec, x);
-    f[10] = encode_level<10>(table, T, dense_mask, x);
-    f[11] = encode_level<11>(table, T, dense_mask, x);
-    f[12] = encode_level<12>(table, T, dense_mask, x);
-    f[13] = encode_level<13>(table, T, dense_mask, x);
-    f[14] = encode_level<14>(table, T, dense_mask, x);
-    f[15] = encode_level<15>(table, T, dense_mask, x);
+    f[0] = encode_level_any<0, kRec>(table, rec, T, dense_mask, x);
+    f[1] = encode_level_any<1, kRec>(table, rec, T, dense_mask, x);
+    f[2] = encode_level_any<2, kRec>(table, rec, T, dense_mask, x);
+    f[3] = encode_level_any<3, kRec>(table, rec, T, dense_mask, x);
+    f[4] = encode_level_any<4, kRec>(table, rec, T, dense_mask, x);
+    f[5] = encode_level_any<5, kRec>(table, rec, T, dense_mask, x);
+    f[6] = encode_level_any<6, kRec>(table, rec, T, dense_mask, x);
+    f[7] = encode_level_any<7, kRec>(table, rec, T, dense_mask, x);
+    f[8] = encode_level_any<8, kRec>(table, rec, T, dense_mask, x);
+    f[9] = encode_level_any<9, kRec>(table, rec, T, dense_mask, x);
+    f[10] = encode_level_any<10, kRec>(table, rec, T, dense_mask, x);
+    f[11] = encode_level_any<11, kRec>(table, rec, T, dense_mask, x);
+    f[12] = encode_level_any<12, kRec>(table, rec, T, dense_mask, x);
+    f[13] = encode_level_any<13, kRec>(table, rec, T, dense_mask, x);
+    f[14] = encode_level_any<14, kRec>(table, rec, T, dense_mask, x);
+    f[15] = encode_level_any<15, kRec>(table, rec, T, dense_mask, x);
   }
 #pragma unroll
   for (int c = 0; c < 4; ++c) tc::tmem_st4(taddr + 4 * c, f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]);
@@ -262,7 +270,7 @@ __device__ __forceinline__ void skip_empty(const DevScene& sc, Slot& q) {
   while (q.ei < q.n && !occupied(sc.occ, sample_pos(q.o, q.d, fmaf((float)q.ei + 0.5f, kDt, q.ts)))) ++q.ei;
 }
 
-template <class Src>
+template <class Src, int kRec>
 __global__ void __launch_bounds__(kTcThreads, 1)
 march_tc_kernel(const __grid_constant__ Src src, const DevScene sc, const DevScratch s) {
   const ViewBatch& vb = src.get();
@@ -508,7 +516,7 @@ march_tc_kernel(const __grid_constant__ Src src, const DevScene sc, const DevScr
       uint32_t tag = 0;
       const float t = has ? fmaf((float)q.ei + 0.5f, kDt, q.ts) : 0.0f;
       const float3 x = sample_pos(q.o, q.d, t);
-      encode_all(sc.table16, sc.rec16, sc.T, sc.dense_mask, x, has, enc_cols + 16 * b + lane_off);
+      encode_all<kRec>(sc.table16, sc.rec16, sc.T, sc.dense_mask, x, has, enc_cols + 16 * b + lane_off);
       if (has) {
         tag = kTagSample | (q.first ? kTagFirst : 0u);
         q.first = false;
@@ -565,10 +573,11 @@ __global__ void pack_tc_weights_kernel(const float* __restrict__ w, uint8_t* __r
 // One thread per cell of the record levels: copies the cell's 8 corner
 // entries (same index rule as encode_level) into its 32-byte record.
 __global__ void build_records_kernel(const __half2* __restrict__ table, uint32_t T, uint32_t dense_mask,
-                                     uint4* __restrict__ rec) {
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < kRecCells; c += gridDim.x * blockDim.x) {
+                                     int rec_levels, uint4* __restrict__ rec) {
+  const uint32_t cells = rec_cell_offset(rec_levels);
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
     int L = 0;
-    while (L + 1 < kRecLevels && c >= rec_cell_offset(L + 1)) ++L;
+    while (L + 1 < rec_levels && c >= rec_cell_offset(L + 1)) ++L;
     const uint32_t N = (uint32_t)level_res(L), local = c - rec_cell_offset(L);
     const uint32_t ix = local % N, iy = (local / N) % N, iz = local / (N * N);
     uint32_t e[8];
@@ -592,11 +601,12 @@ __global__ void build_records_kernel(const __half2* __restrict__ table, uint32_t
 
 }  // namespace
 
-size_t tc_record_bytes() { return (size_t)kRecCells * 32; }
+size_t tc_record_bytes(int rec_levels) { return (size_t)rec_cell_offset(rec_levels) * 32; }
 
-cudaError_t launch_build_records(const __half2* table16, uint32_t T, uint32_t dense_mask, uint4* rec,
+cudaError_t launch_build_records(const __half2* table16, uint32_t T, uint32_t dense_mask, int rec_levels, uint4* rec,
                                  cudaStream_t stream) {
-  build_records_kernel<<<2048, 256, 0, stream>>>(table16, T, dense_mask, rec);
+  if (rec_levels != kRecLevelsDefault && rec_levels != kRecLevelsSmall) return cudaErrorInvalidValue;
+  build_records_kernel<<<2048, 256, 0, stream>>>(table16, T, dense_mask, rec_levels, rec);
   return cudaGetLastError();
 }
 
@@ -609,32 +619,42 @@ cudaError_t launch_pack_tc_weights(const float* w32, uint8_t* out, cudaStream_t 
 
 namespace {
 
-template <class Src>
-cudaError_t launch_march_tc_src(const Src& src, const DevScene& scene, const DevScratch& s, int num_sms,
+template <class Src, int kRec>
+cudaError_t launch_march_tc_rec(const Src& src, const DevScene& scene, const DevScratch& s, int num_sms,
                                 cudaStream_t stream) {
   if (!scene.table16 || !scene.rec16 || !scene.tc_weights) return cudaErrorInvalidValue;
   if (s.max_rays > kIdMask) return cudaErrorInvalidValue;  // ray ids share a word with the flags
   static bool attr_set = false;  // idempotent; a race only repeats the calls
   if (!attr_set) {
     cudaError_t e =
-        cudaFuncSetAttribute(march_tc_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRequest);
+        cudaFuncSetAttribute(march_tc_kernel<Src, kRec>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRequest);
     if (e != cudaSuccess) return e;
     // 14 % of 228 KiB selects the 32 KiB configuration, which holds the
     // request: the rest of the SM's 256 KiB stays L1 for the table gathers.
-    e = cudaFuncSetAttribute(march_tc_kernel<Src>, cudaFuncAttributePreferredSharedMemoryCarveout, 14);
+    e = cudaFuncSetAttribute(march_tc_kernel<Src, kRec>, cudaFuncAttributePreferredSharedMemoryCarveout, 14);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   // One CTA per SM is what makes the 512-column TMEM allocation safe: two
   // 1024-thread CTAs fit on an SM only at <= 32 registers per thread.
   cudaFuncAttributes fa;
-  cudaError_t e = cudaFuncGetAttributes(&fa, march_tc_kernel<Src>);
+  cudaError_t e = cudaFuncGetAttributes(&fa, march_tc_kernel<Src, kRec>);
   if (e != cudaSuccess) return e;
   // The setmaxnreg split hands out exactly 1024 x kLaunchRegs registers: a
   // build with a smaller launch allocation would stall the encoders' increase.
   if (fa.numRegs != (int)kLaunchRegs) return cudaErrorInvalidConfiguration;
-  march_tc_kernel<Src><<<num_sms, kTcThreads, kSmemRequest, stream>>>(src, scene, s);
+  march_tc_kernel<Src, kRec><<<num_sms, kTcThreads, kSmemRequest, stream>>>(src, scene, s);
   return cudaGetLastError();
+}
+
+template <class Src>
+cudaError_t launch_march_tc_src(const Src& src, const DevScene& scene, const DevScratch& s, int num_sms,
+                                cudaStream_t stream) {
+  if (scene.rec_levels == kRecLevelsDefault)
+    return launch_march_tc_rec<Src, kRecLevelsDefault>(src, scene, s, num_sms, stream);
+  if (scene.rec_levels == kRecLevelsSmall)
+    return launch_march_tc_rec<Src, kRecLevelsSmall>(src, scene, s, num_sms, stream);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace

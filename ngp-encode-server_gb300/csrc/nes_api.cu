@@ -125,6 +125,7 @@ void nes_config_default(nes_config* cfg) {
   cfg->depth_gray_max = 4.0f;
   cfg->device = 0;
   cfg->max_pixels = 2u * 1920u * 1832u;
+  cfg->record_levels = kRecLevelsDefault;
 }
 
 const char* nes_strerror(int code) {
@@ -154,6 +155,9 @@ int nes_create(const nes_config* cfg, nes_ctx** out) {
   if (cfg->precision != NES_PREC_FP32 && cfg->precision != NES_PREC_FP16_TC) return NES_EINVAL;
   if (cfg->max_pixels == 0 || cfg->max_pixels > (1u << 27)) return NES_EINVAL;
   if (!(cfg->fov_deg > 0.0f && cfg->fov_deg < 180.0f)) return NES_EINVAL;
+  if (cfg->record_levels != 0 && cfg->record_levels != (uint32_t)kRecLevelsDefault &&
+      cfg->record_levels != (uint32_t)kRecLevelsSmall)
+    return NES_EINVAL;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0) return NES_ENODEV;
   if (cudaSetDevice(cfg->device) != cudaSuccess) return NES_ENODEV;
@@ -162,6 +166,7 @@ int nes_create(const nes_config* cfg, nes_ctx** out) {
   if (!c) return NES_ENOMEM;
   c->cfg = *cfg;
   if (!(c->cfg.depth_gray_max > 0.0f)) c->cfg.depth_gray_max = 4.0f;
+  if (c->cfg.record_levels == 0) c->cfg.record_levels = kRecLevelsDefault;
   int rc = NES_OK;
   auto fail = [&](int code) {
     free_ctx(c);
@@ -192,8 +197,11 @@ int nes_create(const nes_config* cfg, nes_ctx** out) {
   if (cfg->precision == NES_PREC_FP16_TC) {
     if ((rc = dalloc(&c->d_table16, entries)) != NES_OK) return fail(rc);
     if (launch_table_to_fp16(c->d_table32, c->d_table16, entries, c->stream) != cudaSuccess) return fail(NES_EIO);
-    if ((rc = dalloc(&c->d_rec16, tc_record_bytes() / sizeof(uint4))) != NES_OK) return fail(rc);
-    if (launch_build_records(c->d_table16, host.T, c->scene.dense_mask, c->d_rec16, c->stream) != cudaSuccess)
+    c->scene.rec_levels = c->cfg.record_levels;
+    if ((rc = dalloc(&c->d_rec16, tc_record_bytes((int)c->cfg.record_levels) / sizeof(uint4))) != NES_OK)
+      return fail(rc);
+    if (launch_build_records(c->d_table16, host.T, c->scene.dense_mask, (int)c->cfg.record_levels, c->d_rec16,
+                             c->stream) != cudaSuccess)
       return fail(NES_EIO);
     if ((rc = dalloc(&c->d_tc_weights, tc_weight_bytes())) != NES_OK) return fail(rc);
     if (launch_pack_tc_weights(c->d_weights, c->d_tc_weights, c->stream) != cudaSuccess) return fail(NES_EIO);
@@ -520,7 +528,8 @@ int nes_scene_set_param(nes_ctx* c, int which, const float* host_in, size_t coun
   if (c->cfg.precision == NES_PREC_FP16_TC) {  // the tensor-core path's derived copies
     if (which == 0) {
       NES_CUDA(launch_table_to_fp16(c->d_table32, c->d_table16, (size_t)kLevels * c->scene.T, c->stream));
-      NES_CUDA(launch_build_records(c->d_table16, c->scene.T, c->scene.dense_mask, c->d_rec16, c->stream));
+      NES_CUDA(launch_build_records(c->d_table16, c->scene.T, c->scene.dense_mask, (int)c->scene.rec_levels,
+                                    c->d_rec16, c->stream));
     } else {
       NES_CUDA(launch_pack_tc_weights(c->d_weights, c->d_tc_weights, c->stream));
     }

@@ -34,17 +34,21 @@ NES_HD constexpr int level_res(int l) {
        : l == 11 ? 561 : l == 12 ? 776 : l == 13 ? 1072 : l == 14 ? 1482 : 2048;
 }
 
-// Levels 0..kRecLevels-1 are also stored as per-cell records of their 8
-// corner entries for the tensor-core march: cells of level l start at
-// rec_cell_offset(l) (N_0^3 + ... + N_{l-1}^3); 40,712,464 cells, 1.30 GB.
-constexpr int kRecLevels = 10;
+// The tensor-core march also stores its coarse levels as per-cell records
+// of their 8 corner entries: each record replaces eight scattered table
+// gathers by one 32-byte read.  Cells of level l start at rec_cell_offset(l)
+// (N_0^3 + ... + N_{l-1}^3).  A context records levels 0..12 by default
+// (751,482,937 cells, 24.0 GB) or, to save device memory, levels 0..9
+// (40,712,464 cells, 1.30 GB).
+constexpr int kRecLevelsDefault = 13;
+constexpr int kRecLevelsSmall = 10;
 NES_HD constexpr uint32_t rec_cell_offset(int l) {
   uint32_t o = 0;
   for (int j = 0; j < l; ++j) o += (uint32_t)level_res(j) * (uint32_t)level_res(j) * (uint32_t)level_res(j);
   return o;
 }
-constexpr uint32_t kRecCells = rec_cell_offset(kRecLevels);
-static_assert(kRecCells == 40712464u, "record cells of levels 0..9");
+static_assert(rec_cell_offset(kRecLevelsDefault) == 751482937u, "record cells of levels 0..12");
+static_assert(rec_cell_offset(kRecLevelsSmall) == 40712464u, "record cells of levels 0..9");
 
 // Spatial-hash primes (Instant-NGP paper, Sec. 3).
 constexpr uint32_t kPrime1 = 2654435761u;

@@ -1,10 +1,10 @@
 // probe.cu -- measured ceilings for the tensor-core march's gather stream.
 //
-// The march's MLP contraction has a tensor-core roofline (MEASURED bf16
-// peak); its other term is the hash-table gather stream: per sample 10
-// per-cell corner records (levels 0-9, 32 bytes each, read as two 16-byte
-// loads) and 6 x 8 scattered 4-byte table entries (levels 10-15), the
-// 512 bytes of algorithmic gathers.  No library figure exists for such a
+// The march's MLP contraction has a tensor-core roofline (the measured bf16
+// peak); its other term is the hash-table gather stream: per sample one
+// per-cell corner record for each of the recorded levels (32 bytes,
+// read as two 16-byte loads) and 8 scattered 4-byte table entries for each
+// level above: the 512 bytes of algorithmic gathers.  No library figure exists for such a
 // stream, so these kernels measure it on the device itself:
 //
 //  - gather_probe_kernel: uniformly random loads of 4, 16 or 32 bytes over a
@@ -92,6 +92,15 @@ __device__ __forceinline__ uint32_t replay_level_tab(const uint32_t* __restrict_
   return acc;
 }
 
+// Level L as the march reads it: a per-cell record if the level is recorded, else
+// eight table entries.
+template <int L>
+__device__ __forceinline__ uint32_t replay_level(const DevScene& sc, const uint32_t* __restrict__ table,
+                                                 const float3& x) {
+  if ((uint32_t)L < sc.rec_levels) return replay_level_rec<L>(sc.rec16, x);
+  return replay_level_tab<L>(table, sc.T, sc.dense_mask, x);
+}
+
 // One thread per ray slot, warps refilled 32 rays at a time (one 4x8 pixel
 // tile) once all their lanes are done, every occupied sample's 10 records
 // and 48 table entries loaded in order, the occupancy bit of every sample
@@ -135,14 +144,12 @@ replay_kernel(const __grid_constant__ InParam<ViewBatch> src, const DevScene sc,
     if (__ballot_sync(0xffffffffu, live) == 0u && exhausted) break;
     if (live) {
       const float3 x = sample_pos(o, d, fmaf((float)ei + 0.5f, kDt, ts));
-      acc ^= replay_level_rec<0>(sc.rec16, x) ^ replay_level_rec<1>(sc.rec16, x) ^
-             replay_level_rec<2>(sc.rec16, x) ^ replay_level_rec<3>(sc.rec16, x) ^
-             replay_level_rec<4>(sc.rec16, x) ^ replay_level_rec<5>(sc.rec16, x) ^
-             replay_level_rec<6>(sc.rec16, x) ^ replay_level_rec<7>(sc.rec16, x) ^
-             replay_level_rec<8>(sc.rec16, x) ^ replay_level_rec<9>(sc.rec16, x);
-      acc ^= replay_level_tab<10>(table, sc.T, sc.dense_mask, x) ^ replay_level_tab<11>(table, sc.T, sc.dense_mask, x) ^
-             replay_level_tab<12>(table, sc.T, sc.dense_mask, x) ^ replay_level_tab<13>(table, sc.T, sc.dense_mask, x) ^
-             replay_level_tab<14>(table, sc.T, sc.dense_mask, x) ^ replay_level_tab<15>(table, sc.T, sc.dense_mask, x);
+      acc ^= replay_level<0>(sc, table, x) ^ replay_level<1>(sc, table, x) ^ replay_level<2>(sc, table, x) ^
+             replay_level<3>(sc, table, x) ^ replay_level<4>(sc, table, x) ^ replay_level<5>(sc, table, x) ^
+             replay_level<6>(sc, table, x) ^ replay_level<7>(sc, table, x) ^ replay_level<8>(sc, table, x) ^
+             replay_level<9>(sc, table, x) ^ replay_level<10>(sc, table, x) ^ replay_level<11>(sc, table, x) ^
+             replay_level<12>(sc, table, x) ^ replay_level<13>(sc, table, x) ^ replay_level<14>(sc, table, x) ^
+             replay_level<15>(sc, table, x);
       ++ei;
       while (ei < n && !occ_at(ei)) ++ei;
       live = ei < n;

@@ -47,7 +47,7 @@ class NesConfig(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_uint64), ("log2_table_size", ctypes.c_uint32),
                 ("precision", ctypes.c_int32), ("fov_deg", ctypes.c_float),
                 ("depth_gray_max", ctypes.c_float), ("device", ctypes.c_int32),
-                ("max_pixels", ctypes.c_uint32)]
+                ("max_pixels", ctypes.c_uint32), ("record_levels", ctypes.c_uint32)]
 
 
 class NesView(ctypes.Structure):

@@ -83,6 +83,10 @@ def test_create_validates_config(nes_lib):
     assert lib.nes_create(ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
     cfg = nes_lib.default_config(fov_deg=180.0)
     assert lib.nes_create(ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
+    for levels in (1, 9, 11, 12, 14, 16):  # records cover levels 0..9 or 0..12 (or the default, 0)
+        cfg = nes_lib.default_config(precision=nes_lib.PREC_FP16_TC, record_levels=levels)
+        assert lib.nes_create(ctypes.byref(cfg), ctypes.byref(h)) == nes_lib.NES_EINVAL
+    assert nes_lib.default_config().record_levels == 13
 
 
 def test_server_create_validates_config(nes_lib):

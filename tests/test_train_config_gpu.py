@@ -9,9 +9,10 @@ shell).  The hand-written gradient is checked
   - against the FP64 oracle's reverse-mode gradient on a 64-ray batch, in
     both modes: FP32 (exact_weight_grads = 1) to relative L2 1e-4 and 1e-3
     of each block's largest entry; the default tensor-core mode (TF32
-    operands) to relative L2 3e-2 per block and, on table entries fed by at
-    least SUPPORT_MIN samples (and on every weight, which sums all samples),
-    to TC_PEAK of the block's largest entry.  Entries fed by one or two
+    operands): each weight block (a sum over every sample) to 1e-2 relative
+    L2 and 1e-2 of its largest entry, each table level to 3e-2 relative L2
+    and, on entries fed by at least SUPPORT_MIN samples, to 5e-2 of the
+    level's largest entry.  Entries fed by one or two
     samples are left to the L2 bound: where a hidden unit's pre-activation
     lands on the other side of zero in TF32 than in FP32, that sample's whole
     contribution changes."""
@@ -29,6 +30,11 @@ BLOCKS = {"dw1": (0, 2048), "dw2": (2048, 3072), "cw1": (3072, 5120), "cw2": (51
 RES = [16, 22, 30, 42, 58, 80, 111, 153, 212, 294, 406, 561, 776, 1072, 1482, 2048]
 P1, P2 = np.uint32(2654435761), np.uint32(805459861)
 SUPPORT_MIN = 8
+# Tensor-core mode against the oracle (measured on this batch: weight blocks
+# 0.2-0.5 % relative L2 and of the block's largest entry; table levels
+# 0.4-1.9 % relative L2, at most 4.5 % of the level's largest entry on
+# entries fed by >= 8 samples, up to 10 % on entries fed by fewer).
+TC_W_REL, TC_W_PEAK = 1e-2, 1e-2
 TC_REL, TC_PEAK = 3e-2, 5e-2
 
 
@@ -133,7 +139,7 @@ def test_gradient_vs_oracle_64_rays(nes_lib, oracle_mod, teacher, cuda, exact):
     for name, (a, b) in BLOCKS.items():
         e = _errs(gw[a:b], ogw[a:b])
         report[name] = e
-        lim = (1e-4, 1e-3) if exact else (TC_REL, TC_PEAK)
+        lim = (1e-4, 1e-3) if exact else (TC_W_REL, TC_W_PEAK)
         if not (e[0] <= lim[0] and e[1] <= lim[1]):
             bad.append((name, e))
     for lvl in range(16):
