@@ -181,6 +181,10 @@ cudaError_t launch_gather_probe(const void* table, uint64_t table_bytes, int loa
 cudaError_t launch_gather_replay(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
                                  uint32_t* sink, cudaStream_t stream) {
   if (!scene.table16 || !scene.rec16) return cudaErrorInvalidValue;
+  // The march's L1 / shared-memory split (32 KiB shared, the rest L1): the
+  // gathers' speed depends on it.
+  cudaError_t e = cudaFuncSetAttribute(replay_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 14);
+  if (e != cudaSuccess) return e;
   replay_kernel<<<num_sms, 512, 0, stream>>>(InParam<ViewBatch>{views}, scene, s, sink);
   return cudaGetLastError();
 }
