@@ -425,8 +425,9 @@ def roofline_terms(head, kind, tf_sust, src, hbm):
 def measure_gather_ceilings(r, views, flush, stream, dev, reps=5):
     """The gather term of the march's roofline, measured on this device:
     the march's own load stream replayed without arithmetic on the same
-    views (nes_probe_gather_replay, L2 flushed before each replay, median),
-    and the random-gather rates of 4-, 16- and 32-byte loads over an
+    views (nes_probe_gather_replay with 512 and with 256 ray slots per SM,
+    L2 flushed before each replay, median per setting, the faster setting
+    kept), and the random-gather rates of 4-, 16- and 32-byte loads over an
     L2-resident 32 MiB table (nes_probe_gather, CUDA events, median of
     `reps` launches)."""
     import ctypes
@@ -437,15 +438,19 @@ def measure_gather_ceilings(r, views, flush, stream, dev, reps=5):
     sink = torch.empty(max(sms * 512, sms * 2048), dtype=torch.int32, device=dev)
     arr = (nes.NesView * len(views))(*views)
     ms = ctypes.c_float(0)
-    rep = []
-    for i in range(reps + 1):
-        flush.zero_()
-        torch.cuda.synchronize()
-        nes.check(lib.nes_probe_gather_replay(r.h, arr, len(views), sink.data_ptr(), sink.numel(), ctypes.byref(ms)),
-                  "nes_probe_gather_replay")
-        if i:
-            rep.append(ms.value)
-    out = {"replay_ms": round(statistics.median(rep), 3)}
+    per = {}
+    for slots in (512, 256):
+        rep = []
+        for i in range(reps + 1):
+            flush.zero_()
+            torch.cuda.synchronize()
+            nes.check(lib.nes_probe_gather_replay(r.h, arr, len(views), slots, sink.data_ptr(), sink.numel(),
+                                                  ctypes.byref(ms)), "nes_probe_gather_replay")
+            if i:
+                rep.append(ms.value)
+        per[slots] = statistics.median(rep)
+    out = {"replay_ms": round(min(per.values()), 3),
+           "replay_ms_by_slots_per_sm": {str(k): round(v, 3) for k, v in per.items()}}
     table = torch.randint(0, 1 << 30, ((32 << 20) // 4,), dtype=torch.int32, device=dev)
     threads, loads = sms * 2048, 256
     for nbytes in (4, 16, 32):

@@ -484,12 +484,13 @@ int nes_selftest_bounded_wait(nes_ctx *ctx, uint32_t poll_limit, int arrive);
  * nes_probe_gather_replay replays the march's own load stream for the views
  * on a tensor-core context -- the same rays, warp refills, sample positions,
  * record and table addresses, with no interpolation, MLP or compositing --
- * and returns its device time (CUDA events) in *replay_ms; sink_dev holds at
- * least (SM count) x 512 words.  Both write nothing but the sink. */
+ * with `threads` (256 or 512) ray slots per SM, and returns its device time
+ * (CUDA events) in *replay_ms; sink_dev holds at least (SM count) x threads
+ * words.  Both write nothing but the sink. */
 int nes_probe_gather(const void *table_dev, uint64_t table_bytes, int load_bytes, uint32_t loads_per_thread,
                      uint32_t threads, uint32_t *sink_dev, void *stream);
-int nes_probe_gather_replay(nes_ctx *ctx, const nes_view *views, int nviews, uint32_t *sink_dev, size_t sink_words,
-                            float *replay_ms);
+int nes_probe_gather_replay(nes_ctx *ctx, const nes_view *views, int nviews, int threads, uint32_t *sink_dev,
+                            size_t sink_words, float *replay_ms);
 
 /* Per-kernel timing with CUDA events recorded on the stream the kernels
  * run on (the reference's ScopedTimer averages, src/server.cpp:172-190,

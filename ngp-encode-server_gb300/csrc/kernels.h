@@ -123,12 +123,12 @@ cudaError_t launch_bounded_wait_probe(uint32_t poll_limit, int arrive, uint32_t*
 // random loads of load_bytes (4, 16, or 32 as two 16-byte loads) over
 // table_bytes (table_bytes / load_bytes a power of two), XOR-folded into
 // sink[thread].  gather_replay: the march's own load stream over the rays
-// already generated in s (num_sms CTAs of 512 threads; sink holds num_sms *
-// 512 words).
+// already generated in s (num_sms CTAs of `threads` = 256 or 512 threads;
+// sink holds num_sms * threads words).
 cudaError_t launch_gather_probe(const void* table, uint64_t table_bytes, int load_bytes, uint32_t loads_per_thread,
                                 uint32_t* sink, uint32_t threads, cudaStream_t stream);
 cudaError_t launch_gather_replay(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
-                                 uint32_t* sink, cudaStream_t stream);
+                                 int threads, uint32_t* sink, cudaStream_t stream);
 
 // FP32 -> FP16 table conversion (level-major, same indexing).
 cudaError_t launch_table_to_fp16(const float2* src, __half2* dst, size_t n, cudaStream_t stream);

@@ -590,11 +590,11 @@ int nes_probe_gather(const void* table_dev, uint64_t table_bytes, int load_bytes
   return e == cudaSuccess ? NES_OK : (e == cudaErrorInvalidValue ? NES_EINVAL : NES_EIO);
 }
 
-int nes_probe_gather_replay(nes_ctx* c, const nes_view* views, int nviews, uint32_t* sink_dev, size_t sink_words,
-                            float* replay_ms) {
+int nes_probe_gather_replay(nes_ctx* c, const nes_view* views, int nviews, int threads, uint32_t* sink_dev,
+                            size_t sink_words, float* replay_ms) {
   if (!c || !views || !sink_dev || !replay_ms) return NES_EINVAL;
-  if (c->cfg.precision != NES_PREC_FP16_TC) return NES_EINVAL;
-  if (sink_words < (size_t)c->num_sms * 512) return NES_EINVAL;
+  if (c->cfg.precision != NES_PREC_FP16_TC || (threads != 256 && threads != 512)) return NES_EINVAL;
+  if (sink_words < (size_t)c->num_sms * (size_t)threads) return NES_EINVAL;
   std::lock_guard<std::mutex> lock(c->mu);
   NES_CUDA(cudaSetDevice(c->cfg.device));
   ViewBatch vb;
@@ -614,7 +614,7 @@ int nes_probe_gather_replay(nes_ctx* c, const nes_view* views, int nviews, uint3
   cudaError_t e = cudaMemsetAsync(c->scratch.counters, 0, kCtrWords * sizeof(uint32_t), c->stream);
   if (e == cudaSuccess) e = launch_raygen(vb, c->scratch, c->stream);
   if (e == cudaSuccess) e = cudaEventRecord(ev[0], c->stream);
-  if (e == cudaSuccess) e = launch_gather_replay(vb, c->scene, c->scratch, c->num_sms, sink_dev, c->stream);
+  if (e == cudaSuccess) e = launch_gather_replay(vb, c->scene, c->scratch, c->num_sms, threads, sink_dev, c->stream);
   if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
   if (e == cudaSuccess) e = cudaEventElapsedTime(replay_ms, ev[0], ev[1]);

@@ -104,8 +104,8 @@ __device__ __forceinline__ uint32_t replay_level(const DevScene& sc, const uint3
 // One thread per ray slot, warps refilled 32 rays at a time (one 4x8 pixel
 // tile) once all their lanes are done, every occupied sample's 10 records
 // and 48 table entries loaded in order, the occupancy bit of every sample
-// read as the march reads it; 512 threads per CTA, one CTA per SM, as many
-// slots as the march's encoder threads.
+// read as the march reads it; one CTA per SM of 512 threads (as many slots
+// as the march's encoder threads) or 256 (half as many loads in flight).
 __global__ void __launch_bounds__(512, 1)
 replay_kernel(const __grid_constant__ InParam<ViewBatch> src, const DevScene sc, const DevScratch s,
               uint32_t* __restrict__ sink) {
@@ -179,13 +179,14 @@ cudaError_t launch_gather_probe(const void* table, uint64_t table_bytes, int loa
 }
 
 cudaError_t launch_gather_replay(const ViewBatch& views, const DevScene& scene, const DevScratch& s, int num_sms,
-                                 uint32_t* sink, cudaStream_t stream) {
+                                 int threads, uint32_t* sink, cudaStream_t stream) {
+  if (threads != 256 && threads != 512) return cudaErrorInvalidValue;
   if (!scene.table16 || !scene.rec16) return cudaErrorInvalidValue;
   // The march's L1 / shared-memory split (32 KiB shared, the rest L1): the
   // gathers' speed depends on it.
   cudaError_t e = cudaFuncSetAttribute(replay_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 14);
   if (e != cudaSuccess) return e;
-  replay_kernel<<<num_sms, 512, 0, stream>>>(InParam<ViewBatch>{views}, scene, s, sink);
+  replay_kernel<<<num_sms, threads, 0, stream>>>(InParam<ViewBatch>{views}, scene, s, sink);
   return cudaGetLastError();
 }
 

@@ -139,7 +139,7 @@ _SIGS = {
                            ctypes.POINTER(ctypes.c_uint16), ctypes.POINTER(ctypes.c_uint64)]),
     "nes_selftest_bounded_wait": (_I, [_P, ctypes.c_uint32, _I]),
     "nes_probe_gather": (_I, [_P, ctypes.c_uint64, _I, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
-    "nes_probe_gather_replay": (_I, [_P, _P, _I, _P, _SZ, ctypes.POINTER(ctypes.c_float)]),
+    "nes_probe_gather_replay": (_I, [_P, _P, _I, _I, _P, _SZ, ctypes.POINTER(ctypes.c_float)]),
     "nes_set_profiling": (_I, [_P, _I]),
     "nes_last_timings": (_I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "nes_scene_generate": (_I, [ctypes.c_uint64, ctypes.c_uint32, _P, _P]),

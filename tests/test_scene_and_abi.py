@@ -207,7 +207,7 @@ def test_probe_and_selftest_entries_reject_bad_arguments_without_gpu(nes_lib):
     assert lib.nes_probe_gather(table, 3 << 20, 4, 16, 256, sink, None) == EINVAL      # not a power of two
     assert lib.nes_probe_gather(table, 1 << 25, 16, 16, 100, sink, None) == EINVAL     # threads % 256
     ms = ctypes.c_float(0)
-    assert lib.nes_probe_gather_replay(None, None, 1, sink, 1 << 20, ctypes.byref(ms)) == EINVAL
+    assert lib.nes_probe_gather_replay(None, None, 1, 512, sink, 1 << 20, ctypes.byref(ms)) == EINVAL
     assert lib.nes_selftest_bounded_wait(None, 100, 0) == EINVAL
     ls = (ctypes.c_int * 3)(64, 32, 32)
     views = (nes_lib.NesView * 2)()
