@@ -43,13 +43,16 @@ W, H, FOV, NPOSES, RADIUS = 1920, 1080, 90.0, 100, 1.5
 FLOP_PER_SAMPLE = 18688          # 2 x 9,344 MLP multiply-adds
 GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
 # dram__bytes_read.sum + dram__bytes_write.sum of one full 1920x1080 march
-# launch (one ncu capture of that launch per kernel, the command
-# `bench.py --steps 1 --warmup 1 --precision <tc|fp32> --no-extras`).
-DRAM_BYTES_PER_LAUNCH = {"fp16": 2815.030e6 + 18.675e6, "fp32": 73.651e6 + 7.437e6}
-DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full 1920x1080 launch"
-# The tensor-core march's binding unit, from the same capture: L1 data-pipe
-# (LSU) wavefronts as a fraction of their peak rate, averaged over SMs.
-L1_WAVEFRONT_FRAC = {"fp16": 0.694}
+# launch: the tensor-core march with records of levels 0..12 from a 1-pass
+# ncu capture of `bench.py --steps 1 --warmup 1 --precision tc --no-extras
+# --no-cpu-baseline --e2e-steps 1` (42.13 GB + 25.9 MB), the FP32 march from
+# a capture of the same command with --precision fp32.
+DRAM_BYTES_PER_LAUNCH = {"fp16": 42.130e9 + 25.87e6, "fp32": 73.651e6 + 7.437e6}
+DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full 1920x1080 launch (1 pass)"
+# The tensor-core march's binding unit: L1 data-pipe (LSU) wavefronts as a
+# fraction of their peak rate, averaged over SMs, from the full-section
+# capture of a 960x540 request on a context with records of levels 0..9.
+L1_WAVEFRONT_FRAC = {"fp16": 0.664}
 WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
 L2_RULE = "flushed (256 MiB write) before every timed GPU step"
 REC_GB = {10: 1.30, 13: 24.05}  # per-cell corner records of a tensor-core context (32 B per cell)
@@ -412,12 +415,16 @@ def roofline_terms(head, kind, tf_sust, src, hbm):
                 "algorithmic_hbm_bytes": int(algo),
                 "traffic_ratio": round(traffic / algo, 1) if traffic else None,
                 "traffic_note": "algorithmic HBM bytes: the table read once, the ray list (32 B per hitting ray) "
-                                "and the FP32 RGB + depth written (16 B per pixel); the measured excess is the "
-                                "per-cell corner records of levels 7-9 (1.23 GB copy of table entries, read "
-                                "from HBM because they exceed L2)",
+                                "and the FP32 RGB + depth written (16 B per pixel).  The measured excess is "
+                                "by design: the per-cell corner records of levels 7-12 (copies of table "
+                                "entries, 24 GB) are read from HBM, one 32-byte sector per level and sample "
+                                "(~1.7 TB/s, a quarter of HBM bandwidth), in place of eight scattered L1/L2 "
+                                "gathers each; with records of levels 0-9 only (2.8 GB per launch) the march "
+                                "is 6 % slower",
                 "hbm_peak_gbs": hbm,
-                "limiter": "hash-table gathers: L1 data pipe at 69-73% of its wavefront rate, ALU 40%, "
-                           "tensor pipe 11% (ncu capture of one 1920x1080 march launch)",
+                "limiter": "hash-table gathers through L1: L1 data pipe at 66% of its wavefront rate, "
+                           "long-scoreboard stalls dominant, tensor pipe 10%, DRAM 3% (ncu full sections, "
+                           "960x540 request, records of levels 0-9)",
                 "l1_wavefront_frac": L1_WAVEFRONT_FRAC.get(kind)})
     return out
 

@@ -102,16 +102,20 @@ __device__ __forceinline__ uint32_t replay_level(const DevScene& sc, const uint3
 }
 
 // One thread per ray slot, warps refilled 32 rays at a time (one 4x8 pixel
-// tile) once all their lanes are done, every occupied sample's 10 records
-// and 48 table entries loaded in order, the occupancy bit of every sample
-// read as the march reads it; one CTA per SM of 512 threads (as many slots
-// as the march's encoder threads) or 256 (half as many loads in flight).
+// tile) once all their lanes are done, every occupied sample's records and
+// table entries loaded in order, the occupancy bit of every sample read as
+// the march reads it; one CTA per SM of 512 threads (as many slots as the
+// march's encoder threads) or 256.  Like the march's encoder groups, each
+// group of 128 slots advances one sample per step together (a named-barrier
+// step per sample, the march's tile), so rays that are neighbours on screen
+// stay neighbours in t and share the lines they load.
 __global__ void __launch_bounds__(512, 1)
 replay_kernel(const __grid_constant__ InParam<ViewBatch> src, const DevScene sc, const DevScratch s,
               uint32_t* __restrict__ sink) {
   const ViewBatch& vb = src.get();
   const uint32_t nrays = min(s.counters[kCtrRays], s.max_rays);
   const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t group_bar = 1u + (threadIdx.x >> 7);  // 128 threads per group
   const uint32_t* table = reinterpret_cast<const uint32_t*>(sc.table16);
   uint32_t acc = 0;
   bool live = false, exhausted = false;
@@ -141,7 +145,6 @@ replay_kernel(const __grid_constant__ InParam<ViewBatch> src, const DevScene sc,
         live = ei < n;
       }
     }
-    if (__ballot_sync(0xffffffffu, live) == 0u && exhausted) break;
     if (live) {
       const float3 x = sample_pos(o, d, fmaf((float)ei + 0.5f, kDt, ts));
       acc ^= replay_level<0>(sc, table, x) ^ replay_level<1>(sc, table, x) ^ replay_level<2>(sc, table, x) ^
@@ -154,6 +157,19 @@ replay_kernel(const __grid_constant__ InParam<ViewBatch> src, const DevScene sc,
       while (ei < n && !occ_at(ei)) ++ei;
       live = ei < n;
     }
+    // One step per sample for the whole group; it ends when no warp of the
+    // group has a ray left (every thread takes the same number of steps).
+    const bool warp_busy = !exhausted || __ballot_sync(0xffffffffu, live) != 0u;
+    uint32_t more;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(more)
+        : "r"((uint32_t)warp_busy), "r"(group_bar)
+        : "memory");
+    if (!more) break;
   }
   sink[blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }

@@ -149,12 +149,15 @@ def test_gradient_matches_gpu_finite_differences(nes_lib, setup):
         seg = gt[lvl * (1 << LOG2T) * 2:(lvl + 1) * (1 << LOG2T) * 2]
         order = np.argsort(-np.abs(seg))[:4] + lvl * (1 << LOG2T) * 2
         checks += [(0, int(i), gt[i]) for i in order]
+    # Every +-h evaluation for both step sizes in one launch.
+    hs = (1e-3, 1e-4)
+    wh = [c[0] for c in checks] * 4
+    ix = [c[1] for c in checks] * 4
+    dl = [sgn * h for h in hs for sgn in (1.0, -1.0) for _ in checks]
+    ls = t.loss_fp64_batch(pairs, wh, ix, dl).reshape(len(hs), 2, len(checks))
     bad = []
-    for which, idx, g in checks:
-        errs = []
-        for h in (1e-3, 1e-4):
-            fd = (t.loss_fp64(pairs, which, idx, h) - t.loss_fp64(pairs, which, idx, -h)) / (2 * h)
-            errs.append(abs(fd - g))
+    for j, (which, idx, g) in enumerate(checks):
+        errs = [abs((ls[k, 0, j] - ls[k, 1, j]) / (2 * h) - g) for k, h in enumerate(hs)]
         if min(errs) > 1e-3 * abs(g) + 1e-9:
             bad.append((which, idx, g, min(errs)))
     assert not bad, bad
