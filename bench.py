@@ -49,10 +49,18 @@ GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
 # a capture of the same command with --precision fp32.
 DRAM_BYTES_PER_LAUNCH = {"fp16": 42.130e9 + 25.87e6, "fp32": 73.651e6 + 7.437e6}
 DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full 1920x1080 launch (1 pass)"
-# The tensor-core march's binding unit: L1 data-pipe (LSU) wavefronts as a
-# fraction of their peak rate, averaged over SMs, from the full-section
-# capture of a 960x540 request on a context with records of levels 0..9.
-L1_WAVEFRONT_FRAC = {"fp16": 0.664}
+# The tensor-core march's binding unit is the L1 data pipe (ncu names it as
+# the limiter: LSU wavefronts at 66 % of peak, long-scoreboard stalls
+# dominant).  Its gather term is stated against that pipe: L1 LSU wavefronts
+# per sample of a full 1920x1080 launch with records of levels 0..12 (1-pass
+# ncu capture of the --precision tc command above: l1tex__data_pipe_lsu_
+# wavefronts.sum / the launch's samples), and the pipe's peak of one wavefront
+# per SM per cycle (l1tex__data_pipe_lsu_wavefronts.sum.peak_sustained = the
+# SM count).
+L1_WF_PER_SAMPLE = {("fp16", 13): 5228328301 / 285031892}  # 18.34
+L1_WF_PER_SM_CYCLE = 1.0
+L1_WF_SOURCE = ("ncu l1tex__data_pipe_lsu_wavefronts.sum of one full 1920x1080 launch (1 pass) / its samples; "
+                "peak = 1 wavefront per SM per cycle x SMs x the median SM clock sampled during the timed steps")
 WORKLOAD = "mono 1920x1080, 100 poses on r=1.5 sphere, 90 deg FOV, seed 0, T=2^19"
 L2_RULE = "flushed (256 MiB write) before every timed GPU step"
 REC_GB = {10: 1.30, 13: 24.05}  # per-cell corner records of a tensor-core context (32 B per cell)
@@ -334,7 +342,8 @@ def run_ours(args):
     head = results[renderer_used]
     hbm, tf_burst, tf_sust, src = load_peaks()
     kind = "fp16" if renderer_used == nes.PREC_FP16_TC else "fp32"
-    roof = roofline_terms(head, kind, tf_sust, src, hbm)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    roof = roofline_terms(head, kind, tf_sust, src, hbm, sms, args.record_levels)
     line = {
         "metric": "Mrays/s (pose->YUV render, all pixels)", "value": round(head["mrays"], 3), "unit": "Mrays/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -370,12 +379,16 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
-def roofline_terms(head, kind, tf_sust, src, hbm):
+def roofline_terms(head, kind, tf_sust, src, hbm, sms, rec_levels):
     """The march's two roofline terms per launch: the MLP contraction
     (18,688 FLOP per sample) against the measured bf16 tensor peak, and the
-    gather stream (512 B per sample) against the march's own load stream
-    replayed on this device with no arithmetic.  `bound` names the term
-    with the larger floor; achieved / peak / frac are that term's."""
+    hash-table gathers (512 B per sample) against the unit that carries
+    them, the L1 data pipe: its wavefronts per sample (ncu) x samples / the
+    launch's CUDA-event time, over one wavefront per SM per cycle at the SM
+    clock sampled during the timed steps.  `bound` names the term with the
+    larger floor; achieved / peak / frac are that term's (the gather term in
+    algorithmic GB/s: its peak is the gather rate at which the L1 pipe would
+    be saturated)."""
     ms, n = head["march_ms"], head["samples_per_step"]
     tflops = n * FLOP_PER_SAMPLE / (ms / 1e3) / 1e12
     t_tensor = n * FLOP_PER_SAMPLE / (tf_sust * 1e12) * 1e3
@@ -388,27 +401,35 @@ def roofline_terms(head, kind, tf_sust, src, hbm):
                       "per_unit": "18,688 FLOP per sample (2 x 9,344 MLP multiply-adds)"},
            "tensor_frac": round(tflops / tf_sust, 5)}
     gbytes = n * GATHER_BYTES[kind]
-    out["gather_achieved_gbs"] = round(gbytes / (ms / 1e3) / 1e9, 1)
+    gbs = gbytes / (ms / 1e3) / 1e9
+    out["gather_achieved_gbs"] = round(gbs, 1)
+    wf = L1_WF_PER_SAMPLE.get((kind, rec_levels)) if (W, H) == (1920, 1080) else None
+    clk = head["clocks"].get("sm_mhz") or head["clocks"].get("sm_max_mhz")
+    bound = "tensor"
+    if wf and clk:
+        ach_wf = wf * n / (ms / 1e3)
+        peak_wf = sms * clk * 1e6 * L1_WF_PER_SM_CYCLE
+        frac = ach_wf / peak_wf
+        out["gather"] = {"achieved": round(gbs, 1), "peak": round(gbs / frac, 1), "unit": "GB/s",
+                         "frac": round(frac, 4), "floor_ms": round(ms * frac, 3),
+                         "unit_limit": "L1 data pipe (LSU wavefronts)",
+                         "l1_wavefronts_per_sample": wf, "l1_wavefronts_per_s": round(ach_wf / 1e9, 2),
+                         "l1_wavefront_peak_per_s": round(peak_wf / 1e9, 2), "rate_unit": "G wavefronts/s",
+                         "sm_mhz": clk, "peak_source": L1_WF_SOURCE,
+                         "per_unit": "512 B per sample (16 levels x 8 corners x 2 FP16 features)"}
+        out["gather_frac"] = out["gather"]["frac"]
+        if ms * frac > t_tensor:
+            bound = "gather"
     g = head.get("gather")
     if g:
-        # The replay ran on pose 0; its floor scales to the mean step by samples.
-        t_replay = g["replay_ms"] * n / head["samples_pose0"]
-        peak = gbytes / (t_replay / 1e3) / 1e9
-        out["gather"] = {"achieved": out["gather_achieved_gbs"], "peak": round(peak, 1), "unit": "GB/s",
-                         "frac": round(t_replay / ms, 4), "floor_ms": round(t_replay, 3),
-                         "peak_source": "measured in this run: the march's own load stream replayed with no "
-                                        "interpolation, MLP or compositing (nes_probe_gather_replay, pose 0, "
-                                        "L2 flushed, scaled to the mean step's samples)",
-                         "per_unit": "512 B per sample (16 levels x 8 corners x 2 FP16 features)",
-                         "random_gathers": {k: v for k, v in g.items() if k.startswith("random")}}
-        out["gather_frac"] = out["gather"]["frac"]
-        bound = "gather" if t_replay > t_tensor else "tensor"
-    else:
-        bound = "tensor"
+        # Supporting measurements: the same load stream replayed alone, and
+        # the hardware's random-gather rate (no locality).
+        out["gather_probes"] = dict(g)
+        out["gather_probes"]["replay_ms_scaled"] = round(g["replay_ms"] * n / head["samples_pose0"], 3)
     term = out["gather"] if bound == "gather" else out["tensor"]
     out.update({"bound": bound, "achieved": term["achieved"], "peak": term["peak"], "unit": term["unit"],
                 "frac": term["frac"]})
-    traffic = DRAM_BYTES_PER_LAUNCH.get(kind) if (W, H) == (1920, 1080) else None
+    traffic = DRAM_BYTES_PER_LAUNCH.get(kind) if (W, H) == (1920, 1080) and rec_levels == 13 else None
     rays = head.get("rays_per_step") or W * H
     algo = (16 << 19) * (2 if kind == "fp16" else 4) * 2 + rays * 32 + W * H * 16
     out.update({"traffic": traffic, "traffic_source": DRAM_SOURCE if traffic else None,
@@ -424,18 +445,16 @@ def roofline_terms(head, kind, tf_sust, src, hbm):
                 "hbm_peak_gbs": hbm,
                 "limiter": "hash-table gathers through L1: L1 data pipe at 66% of its wavefront rate, "
                            "long-scoreboard stalls dominant, tensor pipe 10%, DRAM 3% (ncu full sections, "
-                           "960x540 request, records of levels 0-9)",
-                "l1_wavefront_frac": L1_WAVEFRONT_FRAC.get(kind)})
+                           "960x540 request, records of levels 0-9)"})
     return out
 
 
 def measure_gather_ceilings(r, views, flush, stream, dev, reps=5):
-    """The gather term of the march's roofline, measured on this device:
-    the march's own load stream replayed without arithmetic on the same
-    views (nes_probe_gather_replay with 512 and with 256 ray slots per SM,
-    L2 flushed before each replay, median per setting, the faster setting
-    kept), and the random-gather rates of 4-, 16- and 32-byte loads over an
-    L2-resident 32 MiB table (nes_probe_gather, CUDA events, median of
+    """Gather probes beside the march's roofline: the march's own load
+    stream replayed without arithmetic on the same views
+    (nes_probe_gather_replay, 512 ray slots per SM, L2 flushed before each
+    replay, median), and the random-gather rates of 4-, 16- and 32-byte loads
+    over an L2-resident 32 MiB table (nes_probe_gather, CUDA events, median of
     `reps` launches)."""
     import ctypes
     import torch
@@ -445,19 +464,18 @@ def measure_gather_ceilings(r, views, flush, stream, dev, reps=5):
     sink = torch.empty(max(sms * 512, sms * 2048), dtype=torch.int32, device=dev)
     arr = (nes.NesView * len(views))(*views)
     ms = ctypes.c_float(0)
-    per = {}
-    for slots in (512, 256):
-        rep = []
-        for i in range(reps + 1):
-            flush.zero_()
-            torch.cuda.synchronize()
-            nes.check(lib.nes_probe_gather_replay(r.h, arr, len(views), slots, sink.data_ptr(), sink.numel(),
-                                                  ctypes.byref(ms)), "nes_probe_gather_replay")
-            if i:
-                rep.append(ms.value)
-        per[slots] = statistics.median(rep)
-    out = {"replay_ms": round(min(per.values()), 3),
-           "replay_ms_by_slots_per_sm": {str(k): round(v, 3) for k, v in per.items()}}
+    rep = []
+    for i in range(reps + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        nes.check(lib.nes_probe_gather_replay(r.h, arr, len(views), 512, sink.data_ptr(), sink.numel(),
+                                              ctypes.byref(ms)), "nes_probe_gather_replay")
+        if i:
+            rep.append(ms.value)
+    out = {"replay_ms": round(statistics.median(rep), 3),
+           "replay_note": "the march's load stream alone (same rays, addresses and per-tile pacing, no "
+                          "interpolation, MLP or compositing): it runs no faster than the march, which "
+                          "overlaps its gathers with the MLP warps' work"}
     table = torch.randint(0, 1 << 30, ((32 << 20) // 4,), dtype=torch.int32, device=dev)
     threads, loads = sms * 2048, 256
     for nbytes in (4, 16, 32):

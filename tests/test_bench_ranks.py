@@ -116,3 +116,28 @@ def test_oracle_focal_matches_library(nes_lib):
     for w in (1, 33, 400, 800, 1280, 1920, 4096):
         for fov in (45.5, 60.0, 90.0, 100.0, 120.0):
             assert oracle.focal_from_fov(w, fov) == nes_lib.focal_from_fov(w, fov)
+
+
+def test_roofline_terms_gather_on_l1_pipe(monkeypatch):
+    """The gather term is the L1 data pipe's wavefront rate over its peak
+    (one wavefront per SM per cycle at the sampled clock); `bound` names
+    the term with the larger floor, and the line's frac is that term's."""
+    sys.path.insert(0, REPO)
+    import bench
+    monkeypatch.setitem(bench.L1_WF_PER_SAMPLE, ("fp16", 13), 20.0)
+    n, ms = 1e8, 10.0
+    head = {"march_ms": ms, "raygen_ms": 0.01, "samples_per_step": n, "ms_per_step": ms,
+            "clocks": {"sm_mhz": 2000.0, "sm_max_mhz": 2070.0}, "rays_per_step": 1000}
+    out = bench.roofline_terms(head, "fp16", 1700.0, "measured", 7000.0, 100, 13)
+    wf_rate = 20.0 * n / (ms / 1e3)
+    frac = wf_rate / (100 * 2000e6)
+    assert out["gather"]["frac"] == pytest.approx(frac, rel=1e-3)
+    assert out["gather"]["floor_ms"] == pytest.approx(ms * frac, rel=1e-3)
+    gbs = n * 512 / (ms / 1e3) / 1e9
+    assert out["gather"]["peak"] == pytest.approx(gbs / frac, rel=1e-3)
+    tflops = n * bench.FLOP_PER_SAMPLE / (ms / 1e3) / 1e12
+    assert out["tensor"]["frac"] == pytest.approx(tflops / 1700.0, rel=1e-3)
+    assert out["bound"] == "gather" and out["frac"] == out["gather"]["frac"]
+    # Without a wavefront figure for the configuration only the tensor term is placed.
+    out = bench.roofline_terms(head, "fp16", 1700.0, "measured", 7000.0, 100, 10)
+    assert out["bound"] == "tensor" and "gather" not in out
