@@ -7,10 +7,12 @@
 // Per step:
 //  1. rays: (view, pixel) pairs (drawn from the step seed or given) -> the
 //     FP32 ray set-up of rendering, with the target colour and depth;
-//  2. forward (thread per ray): march once, keeping each evaluated sample's
-//     t, alpha, transmittance and colour in the ray's scratch row; loss;
-//     then walk the samples backwards carrying A = dL/dT_k for each one's
-//     compositing adjoint
+//  2. forward: the rays' occupied steps listed (thread per ray), the FP32
+//     field evaluated at every listed sample (thread per sample), then each
+//     ray composited with early termination (thread per ray), keeping each
+//     evaluated sample's t, alpha, transmittance and colour in the ray's
+//     scratch row; loss; then walk the samples backwards carrying
+//     A = dL/dT_k for each one's compositing adjoint
 //        g_w = g_C . c_k + g_D t_k,   dL/dc_k = g_C w_k,
 //        dL/dsigma_k = dt T_{k+1} (g_w - A_{k+1}),
 //        A_k = g_w alpha_k + A_{k+1} (1 - alpha_k),   A_K = 0,
@@ -98,7 +100,7 @@ __device__ __forceinline__ float* stage_row(float* a, int F, uint32_t s) {
 }
 __host__ __device__ constexpr int soff(int f) { return (f >> 3) * 256 + (f & 7) * 4; }
 
-// Forward: 128-thread blocks, three resident per SM at its 135 registers.
+// Forward evaluation: 128-thread blocks, three resident per SM at its 135 registers.
 // Backward: 256-thread blocks capped at 128 registers, two resident per SM
 // (16 warps) with one shared copy of the weights per block, which leaves
 // L1 for the table gathers.
@@ -151,86 +153,124 @@ __global__ void make_rays_kernel(const int2* __restrict__ pairs, int n, const Tr
 
 struct RayOut {  // composited result of one training ray
   float C0, C1, C2, D;
-  int K;  // evaluated samples, in the ray's scratch row
-  int pad[3];
+  int K;           // evaluated samples up to early termination, in the ray's scratch row
+  uint32_t first;  // the ray's occupied steps in the sample list: [first, first + count)
+  uint32_t count;
+  int pad;
 };
 
-// Forward march, persistent: every lane marches one ray at a time and
-// claims the next ray as soon as its current one ends (one atomic per
-// warp per round of claims), so a warp never idles behind its longest ray.
-// Evaluated samples go to the ray's scratch row scratch[i * kMaxSteps, +K).
+// Forward, in three passes, so that the per-sample FP32 MLP runs with every
+// lane of a warp busy (marched one ray per thread, the lanes whose ray is at
+// an empty step would idle while the others evaluate):
+//  1. enumerate_kernel, thread per ray: the ray's occupied steps in order --
+//     the march's sample set before early termination -- listed contiguously
+//     as (ray, k | step << 16), k the sample's index along the ray;
+//  2. eval_kernel, thread per listed sample: the FP32 encoding and MLPs at
+//     that sample, its t, alpha and colour written to the ray's scratch row k
+//     (a warp's samples are consecutive samples of one or two rays: coherent
+//     gathers);
+//  3. composite_kernel, thread per ray: the ray's rows in order, composited
+//     and stopped at T < kTStop exactly as a one-pass march composites, with
+//     each row's transmittance and the ray's RayOut filled in.
+// Per sample the arithmetic is the one-pass march's; only the samples after
+// an early termination are evaluated and then left unused.
+constexpr uint32_t kListStepShift = 16;
+static_assert(kMaxSteps <= (1 << kListStepShift), "k and step share one word");
+
+__global__ void __launch_bounds__(256)
+enumerate_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, uint2* __restrict__ list,
+                 uint32_t capacity, RayOut* __restrict__ rout, uint32_t* __restrict__ cursor,
+                 uint32_t* __restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31u;
+  TrainRay r{};
+  if (i < n) r = rays[i];
+  const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
+  int cnt = 0;
+  for (int st = 0; st < r.n; ++st)
+    if (occupied(sc.occ, sample_pos(o, d, fmaf((float)st + 0.5f, kDt, r.ts)))) ++cnt;
+  int incl = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, off);
+    if ((int)lane >= off) incl += v;
+  }
+  uint32_t base = 0;
+  if (lane == 31 && incl > 0) base = atomicAdd(cursor, (uint32_t)incl);
+  base = __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - cnt);
+  if (i >= n) return;
+  RayOut ro{};
+  ro.first = base;
+  if (cnt > 0 && (base > capacity || (uint32_t)cnt > capacity - base)) {
+    atomicExch(err, kErrOverflow);
+  } else if (cnt > 0) {
+    ro.count = (uint32_t)cnt;
+    uint32_t k = 0;
+    for (int st = 0; st < r.n; ++st)
+      if (occupied(sc.occ, sample_pos(o, d, fmaf((float)st + 0.5f, kDt, r.ts)))) {
+        list[base + k] = make_uint2((uint32_t)i, k | ((uint32_t)st << kListStepShift));
+        ++k;
+      }
+  }
+  rout[i] = ro;
+}
+
+// Persistent grid-stride over the list; its length is the enumeration's
+// cursor (read on the device: no host round trip between the passes).
 __global__ void __launch_bounds__(kFwdThreads)
-forward_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, ScratchSample* __restrict__ scratch,
-               RayOut* __restrict__ rout, uint32_t* __restrict__ ray_cursor) {
+eval_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ total, uint32_t capacity,
+            const TrainRay* __restrict__ rays, const DevScene sc, ScratchSample* __restrict__ scratch) {
   extern __shared__ float4 smem_raw[];
   SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
   load_weights32(W, sc.weights);
   __syncthreads();
-  const unsigned lane = threadIdx.x & 31u;
-  bool live = false, exhausted = false;
-  int ray = 0, nst = 0, step = 0, K = 0;
-  float3 o = make_float3(0.0f, 0.0f, 0.0f), d = o;
-  float ts = 0.0f, T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f;
-  float sh[16];
-  ScratchSample* row = scratch;
-  for (;;) {
-    const bool want = !live && !exhausted;
-    const unsigned need = __ballot_sync(0xffffffffu, want);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(ray_cursor, (uint32_t)__popc(need));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (want) {
-        const uint32_t mine = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
-        if (mine < (uint32_t)n) {
-          ray = (int)mine;
-          const TrainRay r = rays[ray];
-          o = make_float3(r.ox, r.oy, r.oz);
-          d = make_float3(r.dx, r.dy, r.dz);
-          ts = r.ts;
-          nst = r.n;
-          step = 0;
-          K = 0;
-          T = 1.0f;
-          C0 = C1 = C2 = D = 0.0f;
-          sh16(d, sh);
-          row = scratch + (size_t)ray * kMaxSteps;
-          live = true;
-        } else {
-          exhausted = true;
-        }
-      }
-    }
-    if (!__any_sync(0xffffffffu, live)) break;
-    if (!live) continue;
-    if (step < nst) {
-      const float t = fmaf((float)step + 0.5f, kDt, ts);
-      const float3 x = sample_pos(o, d, t);
-      ++step;
-      if (occupied(sc.occ, x)) {
-        float enc[kEnc];
-        encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
-        float dout[kDOut];
-        density_mlp32(W, enc, dout);
-        const float sigma = expf(dout[0] - 1.0f);
-        const float3 c = colour_mlp32(W, sh, dout);
-        const float alpha = -expm1f(-sigma * kDt);
-        const float w = T * alpha;
-        row[K] = ScratchSample{t, alpha, T, c.x, c.y, c.z, 0.0f, 0.0f};
-        ++K;
-        C0 = fmaf(w, c.x, C0);
-        C1 = fmaf(w, c.y, C1);
-        C2 = fmaf(w, c.z, C2);
-        D = fmaf(w, t, D);
-        T -= w;
-      }
-    }
-    if (step >= nst || T < kTStop) {
-      rout[ray] = RayOut{C0, C1, C2, D, K, {0, 0, 0}};
-      live = false;
-    }
+  const uint32_t m = min(*total, capacity);
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+    const uint2 e = list[j];
+    const TrainRay& r = rays[e.x];
+    const uint32_t k = e.y & ((1u << kListStepShift) - 1u), st = e.y >> kListStepShift;
+    const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
+    const float t = fmaf((float)st + 0.5f, kDt, r.ts);
+    const float3 x = sample_pos(o, d, t);
+    float enc[kEnc];
+    encode_fp32(sc.table32, sc.T, sc.dense_mask, x, enc);
+    float dout[kDOut];
+    density_mlp32(W, enc, dout);
+    const float sigma = expf(dout[0] - 1.0f);
+    float sh[16];
+    sh16(d, sh);
+    const float3 c = colour_mlp32(W, sh, dout);
+    const float alpha = -expm1f(-sigma * kDt);
+    scratch[(size_t)e.x * kMaxSteps + k] = ScratchSample{t, alpha, 0.0f, c.x, c.y, c.z, 0.0f, 0.0f};
   }
+}
+
+__global__ void __launch_bounds__(256)
+composite_kernel(int n, ScratchSample* __restrict__ scratch, RayOut* __restrict__ rout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  RayOut ro = rout[i];
+  ScratchSample* row = scratch + (size_t)i * kMaxSteps;
+  float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f;
+  int K = 0;
+  for (uint32_t k = 0; k < ro.count; ++k) {
+    const ScratchSample q = row[k];
+    const float w = T * q.alpha;
+    row[k].T = T;
+    ++K;
+    C0 = fmaf(w, q.cr, C0);
+    C1 = fmaf(w, q.cg, C1);
+    C2 = fmaf(w, q.cb, C2);
+    D = fmaf(w, q.t, D);
+    T -= w;
+    if (T < kTStop) break;
+  }
+  ro.C0 = C0;
+  ro.C1 = C1;
+  ro.C2 = C2;
+  ro.D = D;
+  ro.K = K;
+  rout[i] = ro;
 }
 
 // Loss and compositing adjoint, thread per ray: the ray's samples are walked
@@ -1242,7 +1282,7 @@ struct nes_trainer {
   ScratchSample* d_scratch = nullptr;  // max_rays * kMaxSteps
   SampleRec* d_recs = nullptr;
   uint32_t rec_capacity = 0;
-  uint32_t* d_ctr = nullptr;  // [0] record cursor, [1] error word, [2] ray cursor
+  uint32_t* d_ctr = nullptr;  // [0] record cursor, [1] error word, [2] sample-list cursor
   RayOut* d_rout = nullptr;
   double* d_loss = nullptr;
   float2* d_gtable = nullptr;
@@ -1251,7 +1291,7 @@ struct nes_trainer {
   float* d_stage = nullptr;
   uint8_t* d_bimg = nullptr;  // TF32 weight images of backward_tc_kernel
   uint32_t chunk = 0;
-  int fwd_blocks = 0;  // persistent forward grid: SMs x resident blocks
+  int fwd_blocks = 0;  // persistent eval_kernel grid: SMs x resident blocks
   uint64_t steps = 0;
   uint64_t last_samples = 0;
   // Phase events on the trainer's stream: 0 forward start, 1 forward end,
@@ -1303,8 +1343,17 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   TR_CUDA(cudaMemsetAsync(t->d_ctr, 0, sizeof(uint32_t), t->st));  // the error word is cleared by the caller
   TR_CUDA(cudaMemsetAsync(t->d_ctr + 2, 0, sizeof(uint32_t), t->st));
   TR_CUDA(cudaEventRecord(t->ev[0], t->st));
-  forward_kernel<<<t->fwd_blocks, kFwdThreads, kSmemW, t->st>>>(t->d_rays, n, c->scene, t->d_scratch, t->d_rout,
-                                                             t->d_ctr + 2);
+  // The sample list lives in the records' buffer until the adjoint (after
+  // the composite) writes the records there.
+  uint2* list = reinterpret_cast<uint2*>(t->d_recs);
+  const uint32_t list_capacity = t->rec_capacity;  // SampleRec slots hold at least as many uint2
+  enumerate_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(t->d_rays, n, c->scene, list, list_capacity, t->d_rout,
+                                                       t->d_ctr + 2, t->d_ctr + 1);
+  TR_CUDA(cudaGetLastError());
+  eval_kernel<<<t->fwd_blocks, kFwdThreads, kSmemW, t->st>>>(list, t->d_ctr + 2, list_capacity, t->d_rays, c->scene,
+                                                          t->d_scratch);
+  TR_CUDA(cudaGetLastError());
+  composite_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(n, t->d_scratch, t->d_rout);
   TR_CUDA(cudaGetLastError());
   adjoint_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(t->d_rays, t->d_rout, n, t->d_scratch, t->d_recs,
                                                      t->rec_capacity, t->d_ctr, t->d_ctr + 1, t->d_loss,
@@ -1483,7 +1532,7 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaMemset(t->d_vw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
       cudaMemset(t->d_ctr, 0, 4 * sizeof(uint32_t)) != cudaSuccess)
     return fail(NES_EIO);
-  if (cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess ||
+  if (cudaFuncSetAttribute(eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemW) != cudaSuccess ||
       cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess ||
       cudaFuncSetAttribute(dw_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(DwTcSmem)) !=
           cudaSuccess ||
@@ -1496,7 +1545,7 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
     if (cudaFuncGetAttributes(&fa, backward_tc_kernel) != cudaSuccess || fa.numRegs <= 64) return fail(NES_EIO);
   }
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_kernel, kFwdThreads, kSmemW) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_kernel, kFwdThreads, kSmemW) != cudaSuccess)
     return fail(NES_EIO);
   t->fwd_blocks = ctx->num_sms * (per_sm < 1 ? 1 : per_sm);
   *out = t;
