@@ -289,7 +289,11 @@ typedef struct nes_train_config {
   uint32_t batch_rays;  /* rays per step (2^18 in the refit configuration) */
   float lr, beta1, beta2, eps;
   float depth_weight;
-  int32_t exact_weight_grads; /* 0: weight gradients as TF32 tensor-core GEMMs (tcgen05), 1: FP32 CUDA cores */
+  /* 0 (default): the per-sample MLP on the tensor cores (tcgen05) -- the
+   * forward's field evaluation as 3xTF32 products (FP32-level loss), the
+   * backward's recompute, backpropagation and weight-gradient GEMMs in TF32;
+   * 1: everything in FP32 on the CUDA cores (the strict parity mode). */
+  int32_t exact_weight_grads;
 } nes_train_config;
 
 /* lr 1e-2, betas (0.9, 0.99), eps 1e-15, depth weight 0.1, 2^18 rays,

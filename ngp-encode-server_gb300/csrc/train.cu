@@ -219,7 +219,7 @@ enumerate_kernel(const TrainRay* __restrict__ rays, int n, const DevScene sc, ui
 // cursor (read on the device: no host round trip between the passes).
 __global__ void __launch_bounds__(kFwdThreads)
 eval_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ total, uint32_t capacity,
-            const TrainRay* __restrict__ rays, const DevScene sc, ScratchSample* __restrict__ scratch) {
+            const TrainRay* __restrict__ rays, int n, const DevScene sc, ScratchSample* __restrict__ scratch) {
   extern __shared__ float4 smem_raw[];
   SmemWeights32& W = *reinterpret_cast<SmemWeights32*>(smem_raw);
   load_weights32(W, sc.weights);
@@ -227,8 +227,9 @@ eval_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ total, 
   const uint32_t m = min(*total, capacity);
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
     const uint2 e = list[j];
-    const TrainRay& r = rays[e.x];
     const uint32_t k = e.y & ((1u << kListStepShift) - 1u), st = e.y >> kListStepShift;
+    if (e.x >= (uint32_t)n || k >= (uint32_t)kMaxSteps) continue;  // only after an overflow (flagged)
+    const TrainRay& r = rays[e.x];
     const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
     const float t = fmaf((float)st + 0.5f, kDt, r.ts);
     const float3 x = sample_pos(o, d, t);
@@ -1113,6 +1114,205 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
 }
 constexpr int kBtSmem = (int)kBtImageBytes + 8 * (kBtGroups + 1) + 16;
 
+// ---------------- the forward's field evaluation on the tensor cores, 3xTF32 ----------------
+// eval_kernel's work as tcgen05 kind::tf32 products at FP32-level accuracy:
+// every operand is split into its TF32 rounding (hi) and the FP32 remainder
+// (lo), and each layer accumulates A_hi B_hi + A_lo B_hi + A_hi B_lo in FP32.
+// The dropped A_lo B_lo term and the remainders' own TF32 truncation are
+// below 2^-21 of each product, so the loss keeps the FP32 evaluation's value
+// (plain TF32 products would move it by ~1e-3 relative: a refit whose
+// rendered colour sits within 1e-2 of the target then sees a few per cent of
+// error in its loss and adjoints).  One CTA per SM, two independent groups of
+// 4 warps; a group takes 128 listed samples at a time (thread = sample = TMEM
+// lane), writes each layer's input as A_hi and A_lo into TMEM, one thread
+// issues the three K-chains against the weight images' high and low parts in
+// shared memory, and every thread reads its row of D back for the
+// elementwise step (ReLU, exp, SH, sigmoid) and the next layer's input.
+constexpr int kEtGroups = 2;
+constexpr int kEtThreads = 128 * kEtGroups;
+constexpr uint32_t kEtColsPerGroup = 256;   // A_hi: 0..63, A_lo: 64..127, D: 128..191
+constexpr uint32_t kFwdImageBytes = 40960;  // bt_image 0..4: dW1, dW2, cW1, cW2, cW3
+static_assert(bt_image(5).off == kFwdImageBytes, "forward images first");
+constexpr uint32_t kEtImageBytes = 2 * kFwdImageBytes;  // high parts, then low parts
+constexpr int kEtSmem = (int)kEtImageBytes + 8 * (kEtGroups + 1) + 16;
+
+__device__ __forceinline__ float tf32_hi(float v) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return __uint_as_float(r);
+}
+
+// The forward images' high and low parts from the FP32 weights.
+__global__ void pack_et_images_kernel(const float* __restrict__ w, uint8_t* __restrict__ img) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kFwdImageBytes / 4) return;
+  int i = 0;
+  while (i + 1 < 5 && e >= bt_image(i + 1).off / 4) ++i;
+  const BtImage b = bt_image(i);
+  const uint32_t local = e - b.off / 4;
+  const int n = (int)(local / b.K), k = (int)(local % b.K);
+  const float v = bt_value(w, i, n, k), hi = tf32_hi(v);
+  const uint32_t o = b.off + tf32_off(n, k, (int)b.K);
+  *reinterpret_cast<float*>(img + o) = hi;
+  *reinterpret_cast<float*>(img + kFwdImageBytes + o) = v - hi;
+}
+
+__global__ void __launch_bounds__(kEtThreads, 1)
+eval_tc_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ total, uint32_t capacity,
+               const TrainRay* __restrict__ rays, int n, const DevScene sc, const uint8_t* __restrict__ images,
+               ScratchSample* __restrict__ scratch, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(128) uint8_t smem_et[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_et + kEtImageBytes);  // [group] mma, [kEtGroups] images
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kEtGroups + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, row = tid & 127;
+  if (tid == 0) {
+    for (int k = 0; k <= kEtGroups; ++k) tc::mbar_init(bars + k, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, kEtColsPerGroup * kEtGroups);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tslot;
+  bool fail = false;
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(bars + kEtGroups, kEtImageBytes);
+    tc::bulk_g2s(smem_et, images, kEtImageBytes, bars + kEtGroups);
+    fail = !tc::mbar_wait(bars + kEtGroups, 0);
+  }
+  fail = __syncthreads_or(fail);
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+  const uint32_t hi_col = tmem + g * kEtColsPerGroup, lo_col = hi_col + 64, d_col = hi_col + 128;
+  const uint32_t hi_row = hi_col + lane_off, lo_row = lo_col + lane_off, d_row = d_col + lane_off;
+  const uint32_t sB = tc::smem_addr(smem_et);
+  const uint32_t gbar = 1 + g;
+  uint64_t* mbar = bars + g;
+  uint32_t pm = 0;
+  bool ok = true;
+  // The layer input x[0..K) -> A_hi, A_lo (no wait: the next mma() waits).
+  auto put = [&](const float* x, int K) {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      if (c * 32 >= K) break;
+      uint32_t uh[32], ul[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const float h = tf32_hi(x[32 * c + j]);
+        uh[j] = __float_as_uint(h);
+        ul[j] = __float_as_uint(x[32 * c + j] - h);
+      }
+      tc::tmem_st32_nowait(hi_row + 32 * c, uh);
+      tc::tmem_st32_nowait(lo_row + 32 * c, ul);
+    }
+  };
+  // D[:, :N] = A B_i^T at 3xTF32; the group learns of any failed wait here
+  // and stops as a whole.
+  auto mma = [&](int i) -> bool {
+    tc::tmem_wait_st();
+    tc::fence_before();
+    if (tc::named_sync_or(gbar, 128, !ok)) return false;
+    const BtImage b = bt_image(i);
+    if (row == 0) {
+      tc::fence_after();
+      const uint32_t idesc = tc::idesc_tf32_f32(128, (int)b.N);
+      const uint32_t steps = b.K / 8;
+      for (uint32_t j = 0; j < steps; ++j)
+        tc::mma_tf32_at(d_col, hi_col + 8 * j, tc::sdesc(sB + b.off + 256 * j, 128, b.K * 32), idesc, j > 0 ? 1u : 0u);
+      for (uint32_t j = 0; j < steps; ++j)
+        tc::mma_tf32_at(d_col, lo_col + 8 * j, tc::sdesc(sB + b.off + 256 * j, 128, b.K * 32), idesc, 1u);
+      for (uint32_t j = 0; j < steps; ++j)
+        tc::mma_tf32_at(d_col, hi_col + 8 * j, tc::sdesc(sB + kFwdImageBytes + b.off + 256 * j, 128, b.K * 32),
+                        idesc, 1u);
+      tc::mma_commit(mbar);
+    }
+    ok = tc::mbar_wait(mbar, pm) && ok;
+    pm ^= 1u;
+    tc::fence_after();
+    return true;
+  };
+  // ReLU of D[:, :64] -> x.
+  auto relu64 = [&](float (&x)[64]) {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      float v[32];
+      tc::tmem_ld32(d_row + 32 * c, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[32 * c + j] = fmaxf(v[j], 0.0f);
+    }
+  };
+
+  const uint32_t m = min(*total, capacity);
+  const uint32_t ntiles = (m + 127u) / 128u;
+  if (!fail) {
+    for (uint32_t tile = blockIdx.x * kEtGroups + g; tile < ntiles; tile += gridDim.x * kEtGroups) {
+      const uint32_t j = tile * 128u + (uint32_t)row;
+      const uint2 e = j < m ? list[j] : make_uint2(0xFFFFFFFFu, 0u);
+      const uint32_t ray = e.x, k = e.y & ((1u << kListStepShift) - 1u);
+      // (an out-of-range entry exists only after an overflow, which is flagged)
+      const bool valid = j < m && ray < (uint32_t)n && k < (uint32_t)kMaxSteps;
+      float t = 0.0f;
+      float3 d = make_float3(0.0f, 0.0f, 1.0f);
+      float x[64];
+      if (valid) {
+        const TrainRay& r = rays[ray];
+        t = fmaf((float)(e.y >> kListStepShift) + 0.5f, kDt, r.ts);
+        d = make_float3(r.dx, r.dy, r.dz);
+        float enc[kEnc];
+        encode_fp32(sc.table32, sc.T, sc.dense_mask, sample_pos(make_float3(r.ox, r.oy, r.oz), d, t), enc);
+#pragma unroll
+        for (int q = 0; q < kEnc; ++q) x[q] = enc[q];
+      } else {
+#pragma unroll
+        for (int q = 0; q < kEnc; ++q) x[q] = 0.0f;
+      }
+      put(x, kEnc);
+      if (!mma(0)) break;  // h1 = relu(enc dW1^T)
+      relu64(x);
+      put(x, kHid);
+      if (!mma(1)) break;  // out = h1 dW2^T
+      float sigma;
+      {
+        float out[16];
+        tc::tmem_ld16(d_row, out);
+        sigma = expf(out[0] - 1.0f);
+        float sh[16];
+        sh16(d, sh);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) x[q] = sh[q];
+#pragma unroll
+        for (int q = 0; q < 15; ++q) x[16 + q] = out[1 + q];
+        x[31] = 0.0f;
+      }
+      put(x, kCIn);
+      if (!mma(2)) break;  // g1 = relu(cin cW1^T)
+      relu64(x);
+      put(x, kHid);
+      if (!mma(3)) break;  // g2 = relu(g1 cW2^T)
+      relu64(x);
+      put(x, kHid);
+      if (!mma(4)) break;  // logit = g2 cW3^T
+      float lg[16];
+      tc::tmem_ld16(d_row, lg);
+      // The next tile's first product overwrites D: its sync follows these reads.
+      if (valid) {
+        const float alpha = -expm1f(-sigma * kDt);
+        scratch[(size_t)ray * kMaxSteps + k] =
+            ScratchSample{t, alpha, 0.0f, sigmoidf(lg[0]), sigmoidf(lg[1]), sigmoidf(lg[2]), 0.0f, 0.0f};
+      }
+    }
+  }
+  if (fail || !ok) atomicExch(err, kErrTimeout);
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, kEtColsPerGroup * kEtGroups);
+  }
+}
+
 __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
                             size_t n, float lr, float b1, float b2, float eps, float bc1, float bc2) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -1290,6 +1490,7 @@ struct nes_trainer {
   float *d_mt = nullptr, *d_vt = nullptr, *d_mw = nullptr, *d_vw = nullptr;
   float* d_stage = nullptr;
   uint8_t* d_bimg = nullptr;  // TF32 weight images of backward_tc_kernel
+  uint8_t* d_eimg = nullptr;  // high/low TF32 forward images of eval_tc_kernel
   uint32_t chunk = 0;
   int fwd_blocks = 0;  // persistent eval_kernel grid: SMs x resident blocks
   uint64_t steps = 0;
@@ -1350,8 +1551,15 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   enumerate_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(t->d_rays, n, c->scene, list, list_capacity, t->d_rout,
                                                        t->d_ctr + 2, t->d_ctr + 1);
   TR_CUDA(cudaGetLastError());
-  eval_kernel<<<t->fwd_blocks, kFwdThreads, kSmemW, t->st>>>(list, t->d_ctr + 2, list_capacity, t->d_rays, c->scene,
-                                                          t->d_scratch);
+  if (t->cfg.exact_weight_grads) {
+    eval_kernel<<<t->fwd_blocks, kFwdThreads, kSmemW, t->st>>>(list, t->d_ctr + 2, list_capacity, t->d_rays, n,
+                                                            c->scene, t->d_scratch);
+  } else {  // this step's weights as high/low TF32 operand images
+    pack_et_images_kernel<<<(kFwdImageBytes / 4 + 255) / 256, 256, 0, t->st>>>(c->d_weights, t->d_eimg);
+    TR_CUDA(cudaGetLastError());
+    eval_tc_kernel<<<c->num_sms, kEtThreads, kEtSmem, t->st>>>(list, t->d_ctr + 2, list_capacity, t->d_rays, n,
+                                                             c->scene, t->d_eimg, t->d_scratch, t->d_ctr + 1);
+  }
   TR_CUDA(cudaGetLastError());
   composite_kernel<<<(n + 255) / 256, 256, 0, t->st>>>(n, t->d_scratch, t->d_rout);
   TR_CUDA(cudaGetLastError());
@@ -1365,6 +1573,7 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
   TR_CUDA(cudaMemcpyAsync(loss, t->d_loss, sizeof(double), cudaMemcpyDeviceToHost, t->st));
   TR_CUDA(cudaStreamSynchronize(t->st));
   if (h[1] == kErrOverflow) return NES_ENOMEM;
+  if (h[1] == kErrTimeout) return NES_ETIMEDOUT;
   if (h[1]) return NES_EINVAL;
   const uint32_t total = h[0];
   t->last_samples = total;
@@ -1462,6 +1671,7 @@ void free_trainer(nes_trainer* t) {
   cudaFree(t->d_vw);
   cudaFree(t->d_stage);
   cudaFree(t->d_bimg);
+  cudaFree(t->d_eimg);
   for (cudaEvent_t e : t->ev)
     if (e) cudaEventDestroy(e);
   if (t->st) cudaStreamDestroy(t->st);
@@ -1522,7 +1732,8 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaMalloc(&t->d_mw, kWeightFloats * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&t->d_vw, kWeightFloats * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&t->d_stage, (size_t)t->chunk * kStageFloats * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&t->d_bimg, kBtImageBytes) != cudaSuccess)
+      cudaMalloc(&t->d_bimg, kBtImageBytes) != cudaSuccess ||
+      cudaMalloc(&t->d_eimg, kEtImageBytes) != cudaSuccess)
     return fail(NES_ENOMEM);
   if (cudaMemset(t->d_gtable, 0, nt * sizeof(float)) != cudaSuccess ||
       cudaMemset(t->d_gw, 0, kWeightFloats * sizeof(float)) != cudaSuccess ||
@@ -1536,13 +1747,18 @@ int nes_trainer_create(nes_ctx* ctx, const nes_train_config* cfg, nes_trainer** 
       cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemB) != cudaSuccess ||
       cudaFuncSetAttribute(dw_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(DwTcSmem)) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBtSmem) != cudaSuccess)
+      cudaFuncSetAttribute(backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBtSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(eval_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kEtSmem) != cudaSuccess)
     return fail(NES_EIO);
   {
     // backward_tc_kernel allocates all 512 TMEM columns: one CTA per SM,
     // which its register footprint (512 threads x > 64) guarantees.
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, backward_tc_kernel) != cudaSuccess || fa.numRegs <= 64) return fail(NES_EIO);
+    // eval_tc_kernel too: two of its 256-thread CTAs must not fit an SM's
+    // 65,536 registers.
+    if (cudaFuncGetAttributes(&fa, eval_tc_kernel) != cudaSuccess || fa.numRegs * kEtThreads * 2 <= 65536)
+      return fail(NES_EIO);
   }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_kernel, kFwdThreads, kSmemW) != cudaSuccess)

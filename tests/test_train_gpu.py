@@ -17,7 +17,9 @@ rays the fine levels' entries each gather one or two samples, and a hidden
 unit whose TF32 pre-activation lands on the other side of zero than in FP32
 changes that sample's whole contribution: measured 0.2-1.9 % relative L2 and
 up to 15 % of a block's largest entry, held to ORACLE_TF32 = (3e-2, 0.25).
-The loss, which the FP32 forward computes, keeps the FP32 tolerance."""
+The loss keeps the FP32 tolerance in both modes: the default evaluates the
+forward with 3xTF32 products (TF32 high part and FP32 remainder of every
+operand, three products per layer), FP32-level accuracy."""
 import numpy as np
 import pytest
 
@@ -178,7 +180,10 @@ def test_tensor_core_weight_gradients_match_exact(nes_lib, setup):
         t.close()
         r.close()
     (l1, gt1, gw1), (l0, gt0, gw0) = out[1], out[0]
-    assert l0 == pytest.approx(l1, rel=1e-6)
+    # The tensor-core mode evaluates the forward with 3xTF32 products, the
+    # exact mode in FP32 on the CUDA cores: their losses agree to the bar both
+    # meet against the FP64 oracle (measured: 3e-6 relative on these rays).
+    assert l0 == pytest.approx(l1, rel=1e-5)
     print("tensor-core vs FP32 gradients: table", _errs(gt0, gt1),
           {name: _errs(gw0[a:b], gw1[a:b]) for name, (a, b) in BLOCKS.items()})
     assert _close(gt0, gt1, TF32_REL, TF32_PEAK), _errs(gt0, gt1)
