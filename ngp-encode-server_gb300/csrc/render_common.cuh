@@ -183,28 +183,33 @@ __device__ __forceinline__ void corner_weights(const LevelCell& c, float w[8]) {
   w[7] = xy3 * c.fz;
 }
 
-// FP32 table: level-major float2 entries.
+// Level l of the FP32 table (level-major float2 entries) at x -> its two
+// features.
+__device__ __forceinline__ void encode_level_fp32(const float2* __restrict__ table, uint32_t T, uint32_t dense_mask,
+                                                  const float3& x, int l, float& f0, float& f1) {
+  const int N = level_res(l);
+  const LevelCell c = level_cell(x, N);
+  uint32_t idx[8];
+  corner_indices(c, N, (dense_mask >> l) & 1u, T, idx);
+  float w[8];
+  corner_weights(c, w);
+  const float2* tab = table + (size_t)l * T;
+  float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float2 e = __ldg(tab + idx[k]);
+    a0 = fmaf(w[k], e.x, a0);
+    a1 = fmaf(w[k], e.y, a1);
+  }
+  f0 = a0;
+  f1 = a1;
+}
+
+// All levels of the FP32 table at x.
 __device__ __forceinline__ void encode_fp32(const float2* __restrict__ table, uint32_t T,
                                             uint32_t dense_mask, const float3& x, float feat[kEnc]) {
 #pragma unroll
-  for (int l = 0; l < kLevels; ++l) {
-    const int N = level_res(l);
-    const LevelCell c = level_cell(x, N);
-    uint32_t idx[8];
-    corner_indices(c, N, (dense_mask >> l) & 1u, T, idx);
-    float w[8];
-    corner_weights(c, w);
-    const float2* tab = table + (size_t)l * T;
-    float a0 = 0.0f, a1 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const float2 e = __ldg(tab + idx[k]);
-      a0 = fmaf(w[k], e.x, a0);
-      a1 = fmaf(w[k], e.y, a1);
-    }
-    feat[2 * l] = a0;
-    feat[2 * l + 1] = a1;
-  }
+  for (int l = 0; l < kLevels; ++l) encode_level_fp32(table, T, dense_mask, x, l, feat[2 * l], feat[2 * l + 1]);
 }
 
 // Real spherical harmonics, bands 0..3, orthonormal on the sphere.

@@ -1127,10 +1127,16 @@ constexpr int kBtSmem = (int)kBtImageBytes + 8 * (kBtGroups + 1) + 16;
 // lane), writes each layer's input as A_hi and A_lo into TMEM, one thread
 // issues the three K-chains against the weight images' high and low parts in
 // shared memory, and every thread reads its row of D back for the
-// elementwise step (ReLU, exp, SH, sigmoid) and the next layer's input.
+// elementwise step (ReLU, exp, SH, sigmoid) and the next layer's input.  The
+// table gathers of the group's next tile run while the MMAs of layers 1-4 of
+// the current one do (four levels per layer), into TMEM columns of their own
+// that layer 0 of the next tile reads: only two tiles' worth of warps per SM
+// fit the TMEM, so the gathers' latency is hidden behind the layer chain.
 constexpr int kEtGroups = 2;
 constexpr int kEtThreads = 128 * kEtGroups;
-constexpr uint32_t kEtColsPerGroup = 256;   // A_hi: 0..63, A_lo: 64..127, D: 128..191
+// A_hi: 0..63, A_lo: 64..127, D: 128..191, next tile's encoding E_hi:
+// 192..223, E_lo: 224..255.
+constexpr uint32_t kEtColsPerGroup = 256;
 constexpr uint32_t kFwdImageBytes = 40960;  // bt_image 0..4: dW1, dW2, cW1, cW2, cW3
 static_assert(bt_image(5).off == kFwdImageBytes, "forward images first");
 constexpr uint32_t kEtImageBytes = 2 * kFwdImageBytes;  // high parts, then low parts
@@ -1155,6 +1161,60 @@ __global__ void pack_et_images_kernel(const float* __restrict__ w, uint8_t* __re
   const uint32_t o = b.off + tf32_off(n, k, (int)b.K);
   *reinterpret_cast<float*>(img + o) = hi;
   *reinterpret_cast<float*>(img + kFwdImageBytes + o) = v - hi;
+}
+
+// One listed sample's inputs.
+struct EtSample {
+  uint32_t ray, k;
+  float t;
+  float3 o, d;
+  bool valid;
+};
+
+__device__ __forceinline__ EtSample et_sample(const uint2* __restrict__ list, uint32_t j, uint32_t m,
+                                              const TrainRay* __restrict__ rays, int n) {
+  EtSample q;
+  const uint2 e = j < m ? list[j] : make_uint2(0xFFFFFFFFu, 0u);
+  q.ray = e.x;
+  q.k = e.y & ((1u << kListStepShift) - 1u);
+  // (an out-of-range entry exists only after an overflow, which is flagged)
+  q.valid = j < m && q.ray < (uint32_t)n && q.k < (uint32_t)kMaxSteps;
+  q.t = 0.0f;
+  q.o = make_float3(0.0f, 0.0f, 0.0f);
+  q.d = make_float3(0.0f, 0.0f, 1.0f);
+  if (q.valid) {
+    const TrainRay& r = rays[q.ray];
+    q.t = fmaf((float)(e.y >> kListStepShift) + 0.5f, kDt, r.ts);
+    q.o = make_float3(r.ox, r.oy, r.oz);
+    q.d = make_float3(r.dx, r.dy, r.dz);
+  }
+  return q;
+}
+
+// Levels L0..L0+3 of a sample's encoding -> E_hi / E_lo columns 2 L0 ..
+// 2 L0 + 7 of this thread's lane (no wait).  Every lane of the warp calls it.
+template <int L0>
+__device__ __forceinline__ void et_encode4(const DevScene& sc, const EtSample& q, uint32_t ehi_row,
+                                           uint32_t elo_row) {
+  float f[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) f[j] = 0.0f;
+  if (q.valid) {
+    const float3 x = sample_pos(q.o, q.d, q.t);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) encode_level_fp32(sc.table32, sc.T, sc.dense_mask, x, L0 + j, f[2 * j], f[2 * j + 1]);
+  }
+  uint32_t h[8], l[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float hi = tf32_hi(f[j]);
+    h[j] = __float_as_uint(hi);
+    l[j] = __float_as_uint(f[j] - hi);
+  }
+  tc::tmem_st4(ehi_row + 2 * L0, h[0], h[1], h[2], h[3]);
+  tc::tmem_st4(ehi_row + 2 * L0 + 4, h[4], h[5], h[6], h[7]);
+  tc::tmem_st4(elo_row + 2 * L0, l[0], l[1], l[2], l[3]);
+  tc::tmem_st4(elo_row + 2 * L0 + 4, l[4], l[5], l[6], l[7]);
 }
 
 __global__ void __launch_bounds__(kEtThreads, 1)
@@ -1186,13 +1246,15 @@ eval_tc_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ tota
   fail = __syncthreads_or(fail);
   const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
   const uint32_t hi_col = tmem + g * kEtColsPerGroup, lo_col = hi_col + 64, d_col = hi_col + 128;
+  const uint32_t ehi_col = hi_col + 192, elo_col = hi_col + 224;
   const uint32_t hi_row = hi_col + lane_off, lo_row = lo_col + lane_off, d_row = d_col + lane_off;
+  const uint32_t ehi_row = ehi_col + lane_off, elo_row = elo_col + lane_off;
   const uint32_t sB = tc::smem_addr(smem_et);
   const uint32_t gbar = 1 + g;
   uint64_t* mbar = bars + g;
   uint32_t pm = 0;
   bool ok = true;
-  // The layer input x[0..K) -> A_hi, A_lo (no wait: the next mma() waits).
+  // The layer input x[0..K) -> A_hi, A_lo (no wait: the next issue waits).
   auto put = [&](const float* x, int K) {
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -1208,9 +1270,10 @@ eval_tc_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ tota
       tc::tmem_st32_nowait(lo_row + 32 * c, ul);
     }
   };
-  // D[:, :N] = A B_i^T at 3xTF32; the group learns of any failed wait here
-  // and stops as a whole.
-  auto mma = [&](int i) -> bool {
+  // D[:, :N] = A B_i^T at 3xTF32, A from columns (a_hi, a_lo): every thread
+  // publishes its TMEM writes, one thread issues; the group learns of any
+  // failed wait here and stops as a whole.
+  auto issue = [&](int i, uint32_t a_hi, uint32_t a_lo) -> bool {
     tc::tmem_wait_st();
     tc::fence_before();
     if (tc::named_sync_or(gbar, 128, !ok)) return false;
@@ -1220,18 +1283,20 @@ eval_tc_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ tota
       const uint32_t idesc = tc::idesc_tf32_f32(128, (int)b.N);
       const uint32_t steps = b.K / 8;
       for (uint32_t j = 0; j < steps; ++j)
-        tc::mma_tf32_at(d_col, hi_col + 8 * j, tc::sdesc(sB + b.off + 256 * j, 128, b.K * 32), idesc, j > 0 ? 1u : 0u);
+        tc::mma_tf32_at(d_col, a_hi + 8 * j, tc::sdesc(sB + b.off + 256 * j, 128, b.K * 32), idesc, j > 0 ? 1u : 0u);
       for (uint32_t j = 0; j < steps; ++j)
-        tc::mma_tf32_at(d_col, lo_col + 8 * j, tc::sdesc(sB + b.off + 256 * j, 128, b.K * 32), idesc, 1u);
+        tc::mma_tf32_at(d_col, a_lo + 8 * j, tc::sdesc(sB + b.off + 256 * j, 128, b.K * 32), idesc, 1u);
       for (uint32_t j = 0; j < steps; ++j)
-        tc::mma_tf32_at(d_col, hi_col + 8 * j, tc::sdesc(sB + kFwdImageBytes + b.off + 256 * j, 128, b.K * 32),
+        tc::mma_tf32_at(d_col, a_hi + 8 * j, tc::sdesc(sB + kFwdImageBytes + b.off + 256 * j, 128, b.K * 32),
                         idesc, 1u);
       tc::mma_commit(mbar);
     }
+    return true;
+  };
+  auto wait = [&]() {
     ok = tc::mbar_wait(mbar, pm) && ok;
     pm ^= 1u;
     tc::fence_after();
-    return true;
   };
   // ReLU of D[:, :64] -> x.
   auto relu64 = [&](float (&x)[64]) {
@@ -1246,40 +1311,34 @@ eval_tc_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ tota
 
   const uint32_t m = min(*total, capacity);
   const uint32_t ntiles = (m + 127u) / 128u;
-  if (!fail) {
-    for (uint32_t tile = blockIdx.x * kEtGroups + g; tile < ntiles; tile += gridDim.x * kEtGroups) {
-      const uint32_t j = tile * 128u + (uint32_t)row;
-      const uint2 e = j < m ? list[j] : make_uint2(0xFFFFFFFFu, 0u);
-      const uint32_t ray = e.x, k = e.y & ((1u << kListStepShift) - 1u);
-      // (an out-of-range entry exists only after an overflow, which is flagged)
-      const bool valid = j < m && ray < (uint32_t)n && k < (uint32_t)kMaxSteps;
-      float t = 0.0f;
-      float3 d = make_float3(0.0f, 0.0f, 1.0f);
+  const uint32_t stride = gridDim.x * kEtGroups;
+  uint32_t tile = blockIdx.x * kEtGroups + g;
+  if (!fail && tile < ntiles) {
+    // The first tile's encoding; later tiles' are gathered during the
+    // previous tile's layers.
+    EtSample cur = et_sample(list, tile * 128u + (uint32_t)row, m, rays, n);
+    et_encode4<0>(sc, cur, ehi_row, elo_row);
+    et_encode4<4>(sc, cur, ehi_row, elo_row);
+    et_encode4<8>(sc, cur, ehi_row, elo_row);
+    et_encode4<12>(sc, cur, ehi_row, elo_row);
+    for (; tile < ntiles; tile += stride) {
+      const bool more = tile + stride < ntiles;
+      const EtSample nxt = et_sample(list, (tile + stride) * 128u + (uint32_t)row, more ? m : 0u, rays, n);
       float x[64];
-      if (valid) {
-        const TrainRay& r = rays[ray];
-        t = fmaf((float)(e.y >> kListStepShift) + 0.5f, kDt, r.ts);
-        d = make_float3(r.dx, r.dy, r.dz);
-        float enc[kEnc];
-        encode_fp32(sc.table32, sc.T, sc.dense_mask, sample_pos(make_float3(r.ox, r.oy, r.oz), d, t), enc);
-#pragma unroll
-        for (int q = 0; q < kEnc; ++q) x[q] = enc[q];
-      } else {
-#pragma unroll
-        for (int q = 0; q < kEnc; ++q) x[q] = 0.0f;
-      }
-      put(x, kEnc);
-      if (!mma(0)) break;  // h1 = relu(enc dW1^T)
+      if (!issue(0, ehi_col, elo_col)) break;  // h1 = relu(enc dW1^T)
+      wait();
       relu64(x);
       put(x, kHid);
-      if (!mma(1)) break;  // out = h1 dW2^T
+      if (!issue(1, hi_col, lo_col)) break;  // out = h1 dW2^T
+      et_encode4<0>(sc, nxt, ehi_row, elo_row);
+      wait();
       float sigma;
       {
         float out[16];
         tc::tmem_ld16(d_row, out);
         sigma = expf(out[0] - 1.0f);
         float sh[16];
-        sh16(d, sh);
+        sh16(cur.d, sh);
 #pragma unroll
         for (int q = 0; q < 16; ++q) x[q] = sh[q];
 #pragma unroll
@@ -1287,21 +1346,28 @@ eval_tc_kernel(const uint2* __restrict__ list, const uint32_t* __restrict__ tota
         x[31] = 0.0f;
       }
       put(x, kCIn);
-      if (!mma(2)) break;  // g1 = relu(cin cW1^T)
+      if (!issue(2, hi_col, lo_col)) break;  // g1 = relu(cin cW1^T)
+      et_encode4<4>(sc, nxt, ehi_row, elo_row);
+      wait();
       relu64(x);
       put(x, kHid);
-      if (!mma(3)) break;  // g2 = relu(g1 cW2^T)
+      if (!issue(3, hi_col, lo_col)) break;  // g2 = relu(g1 cW2^T)
+      et_encode4<8>(sc, nxt, ehi_row, elo_row);
+      wait();
       relu64(x);
       put(x, kHid);
-      if (!mma(4)) break;  // logit = g2 cW3^T
+      if (!issue(4, hi_col, lo_col)) break;  // logit = g2 cW3^T
+      et_encode4<12>(sc, nxt, ehi_row, elo_row);
+      wait();
       float lg[16];
       tc::tmem_ld16(d_row, lg);
       // The next tile's first product overwrites D: its sync follows these reads.
-      if (valid) {
+      if (cur.valid) {
         const float alpha = -expm1f(-sigma * kDt);
-        scratch[(size_t)ray * kMaxSteps + k] =
-            ScratchSample{t, alpha, 0.0f, sigmoidf(lg[0]), sigmoidf(lg[1]), sigmoidf(lg[2]), 0.0f, 0.0f};
+        scratch[(size_t)cur.ray * kMaxSteps + cur.k] =
+            ScratchSample{cur.t, alpha, 0.0f, sigmoidf(lg[0]), sigmoidf(lg[1]), sigmoidf(lg[2]), 0.0f, 0.0f};
       }
+      cur = nxt;
     }
   }
   if (fail || !ok) atomicExch(err, kErrTimeout);
