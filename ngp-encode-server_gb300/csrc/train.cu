@@ -254,17 +254,28 @@ composite_kernel(int n, ScratchSample* __restrict__ scratch, RayOut* __restrict_
   ScratchSample* row = scratch + (size_t)i * kMaxSteps;
   float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f;
   int K = 0;
-  for (uint32_t k = 0; k < ro.count; ++k) {
-    const ScratchSample q = row[k];
-    const float w = T * q.alpha;
-    row[k].T = T;
-    ++K;
-    C0 = fmaf(w, q.cr, C0);
-    C1 = fmaf(w, q.cg, C1);
-    C2 = fmaf(w, q.cb, C2);
-    D = fmaf(w, q.t, D);
-    T -= w;
-    if (T < kTStop) break;
+  bool stop = false;
+  // Rows in batches of kBatch, all loaded before the first is used: the
+  // stop test of one sample no longer holds back the next sample's load.
+  constexpr uint32_t kBatch = 8;
+  for (uint32_t k0 = 0; k0 < ro.count && !stop; k0 += kBatch) {
+    ScratchSample q[kBatch];
+#pragma unroll
+    for (uint32_t u = 0; u < kBatch; ++u)
+      if (k0 + u < ro.count) q[u] = row[k0 + u];
+#pragma unroll
+    for (uint32_t u = 0; u < kBatch; ++u) {
+      if (stop || k0 + u >= ro.count) break;
+      const float w = T * q[u].alpha;
+      row[k0 + u].T = T;
+      ++K;
+      C0 = fmaf(w, q[u].cr, C0);
+      C1 = fmaf(w, q[u].cg, C1);
+      C2 = fmaf(w, q[u].cb, C2);
+      D = fmaf(w, q[u].t, D);
+      T -= w;
+      stop = T < kTStop;
+    }
   }
   ro.C0 = C0;
   ro.C1 = C1;
