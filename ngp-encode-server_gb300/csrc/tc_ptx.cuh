@@ -113,6 +113,12 @@ __host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
   return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor, kind::f16 with A = B = BF16 (format 1 in the A
+// and B type fields), D = F32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // Instruction descriptor, kind::tf32: A = B = TF32 (format 2 in the A and B
 // type fields), D = F32, both K-major.
 __host__ __device__ constexpr uint32_t idesc_tf32_f32(int M, int N) {

@@ -609,8 +609,12 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
   }
 }
 
-// ---------------- weight gradients on the tensor cores (kind::tf32) ----------------
-// Per 32-sample tile, two MMA groups, M = 128, K = 32 as four K = 8 steps:
+// ---------------- weight gradients on the tensor cores (kind::f16, BF16 operands) ----------------
+// The tensor-core backward stages its activations and deltas as BF16 (FP32's
+// exponent range, 8-bit mantissa; FP16's range cannot hold the deltas) in the
+// 16-bit operand layout of stage8: half the bytes of FP32 staging written by
+// the backward and read back here, the round trip that bounds both kernels.
+// Per 32-sample tile, two MMA groups, M = 128, K = 32 as two K = 16 steps:
 //   D1[128 x 144] += [enc | cin | h1] (rows = features) x [dh1 | dg1 | dout]^T
 //   D2[128 x  80] += [g1 | g2] x [dg2 | dlog | 0]^T
 // whose diagonal blocks are the five dW^T (D1[enc][dh1] = DW1^T, D1[cin][dg1]
@@ -620,11 +624,12 @@ dw_kernel(const float* __restrict__ act, const float* __restrict__ delta, uint32
 // lane 0 streams tiles into a 3-stage ring with bulk copies (one per array,
 // the staging is already in the operand layout), warp 1 lane 0 issues the
 // MMAs and releases stages by tcgen05.commit, all four warps read D back.
-// The kernel is bound by reading the staging (60,416 B per tile).
+// The kernel is bound by reading the staging (30,208 B per tile).
 constexpr int kTcStages = 3;
-constexpr uint32_t kA1Bytes = 128 * 128, kB1Bytes = 144 * 128, kA2Bytes = 128 * 128, kB2Bytes = 80 * 128;
+// Operand tiles of 32 records, BF16 (64 bytes per feature row).
+constexpr uint32_t kA1Bytes = 128 * 64, kB1Bytes = 144 * 64, kA2Bytes = 128 * 64, kB2Bytes = 80 * 64;
 constexpr uint32_t kStageBytes = kA1Bytes + kB1Bytes + kA2Bytes + kB2Bytes;
-constexpr uint32_t kTileTx = (kEnc + kCIn + kHid + kHid + kHid + kDOut + kHid + kHid + kHid + kFDlog) * 128;
+constexpr uint32_t kTileTx = (kEnc + kCIn + kHid + kHid + kHid + kDOut + kHid + kHid + kHid + kFDlog) * 64;
 constexpr uint32_t kD1Col = 0, kD2Col = 144, kTmemCols = 256;
 constexpr int kDwTcThreads = 128;
 constexpr uint32_t kErrTimeout = 4u;
@@ -653,8 +658,8 @@ dw_tc_kernel(Staging st, uint32_t ntiles, float* __restrict__ dw, uint32_t* __re
     tc::fence_mbar_init();
   }
   // B2 rows 72..79 are never copied: zero in every stage.
-  for (int i = threadIdx.x; i < kTcStages * 256; i += blockDim.x)
-    reinterpret_cast<float*>(S.stage[i / 256] + kA1Bytes + kB1Bytes + kA2Bytes + 72 * 128)[i % 256] = 0.0f;
+  for (int i = threadIdx.x; i < kTcStages * 128; i += blockDim.x)
+    reinterpret_cast<float*>(S.stage[i / 128] + kA1Bytes + kB1Bytes + kA2Bytes + 72 * 64)[i % 128] = 0.0f;
   tc::fence_async_smem();
   if (warp == 1) {
     tc::tmem_alloc(&S.tmem_base, kTmemCols);
@@ -680,16 +685,18 @@ dw_tc_kernel(Staging st, uint32_t ntiles, float* __restrict__ dw, uint32_t* __re
       const size_t t = t0 + i;
       uint64_t* bar = &S.full[sidx];
       tc::mbar_arrive_expect_tx(bar, kTileTx);
-      tc::bulk_g2s(a1, st.enc + t * kEnc * 32, kEnc * 128, bar);
-      tc::bulk_g2s(a1 + kEnc * 128, st.cin + t * kCIn * 32, kCIn * 128, bar);
-      tc::bulk_g2s(a1 + (kEnc + kCIn) * 128, st.h1 + t * kHid * 32, kHid * 128, bar);
-      tc::bulk_g2s(b1, st.dh1 + t * kHid * 32, kHid * 128, bar);
-      tc::bulk_g2s(b1 + kHid * 128, st.dg1 + t * kHid * 32, kHid * 128, bar);
-      tc::bulk_g2s(b1 + 2 * kHid * 128, st.dout + t * kDOut * 32, kDOut * 128, bar);
-      tc::bulk_g2s(a2, st.g1 + t * kHid * 32, kHid * 128, bar);
-      tc::bulk_g2s(a2 + kHid * 128, st.g2 + t * kHid * 32, kHid * 128, bar);
-      tc::bulk_g2s(b2, st.dg2 + t * kHid * 32, kHid * 128, bar);
-      tc::bulk_g2s(b2 + kHid * 128, st.dlog + t * kFDlog * 32, kFDlog * 128, bar);
+      // Tile t of an F-wide BF16 array: F x 64 bytes at byte t x F x 64.
+      auto tile = [&](const float* arr, int F) { return reinterpret_cast<const uint8_t*>(arr) + t * F * 64; };
+      tc::bulk_g2s(a1, tile(st.enc, kEnc), kEnc * 64, bar);
+      tc::bulk_g2s(a1 + kEnc * 64, tile(st.cin, kCIn), kCIn * 64, bar);
+      tc::bulk_g2s(a1 + (kEnc + kCIn) * 64, tile(st.h1, kHid), kHid * 64, bar);
+      tc::bulk_g2s(b1, tile(st.dh1, kHid), kHid * 64, bar);
+      tc::bulk_g2s(b1 + kHid * 64, tile(st.dg1, kHid), kHid * 64, bar);
+      tc::bulk_g2s(b1 + 2 * kHid * 64, tile(st.dout, kDOut), kDOut * 64, bar);
+      tc::bulk_g2s(a2, tile(st.g1, kHid), kHid * 64, bar);
+      tc::bulk_g2s(a2 + kHid * 64, tile(st.g2, kHid), kHid * 64, bar);
+      tc::bulk_g2s(b2, tile(st.dg2, kHid), kHid * 64, bar);
+      tc::bulk_g2s(b2 + kHid * 64, tile(st.dlog, kFDlog), kFDlog * 64, bar);
       ++issued;
     }
     if (!ok) atomicExch(err, kErrTimeout);
@@ -700,7 +707,7 @@ dw_tc_kernel(Staging st, uint32_t ntiles, float* __restrict__ dw, uint32_t* __re
       if (!tc::mbar_wait_sleep(&S.full[i % kTcStages], (i / kTcStages) & 1u)) atomicExch(err, kErrTimeout);
     }
   } else if (warp == 1 && lane == 0) {  // MMA issuer
-    constexpr uint32_t id1 = tc::idesc_tf32_f32(128, 144), id2 = tc::idesc_tf32_f32(128, 80);
+    constexpr uint32_t id1 = tc::idesc_bf16_f32(128, 144), id2 = tc::idesc_bf16_f32(128, 80);
     for (uint32_t i = 0; i < my; ++i) {
       const int sidx = (int)(i % kTcStages);
       if (!tc::mbar_wait_sleep(&S.full[sidx], (i / kTcStages) & 1u)) {
@@ -710,10 +717,10 @@ dw_tc_kernel(Staging st, uint32_t ntiles, float* __restrict__ dw, uint32_t* __re
       tc::fence_after();
       const uint32_t a1 = tc::smem_addr(S.stage[sidx]), b1 = a1 + kA1Bytes, a2 = b1 + kB1Bytes, b2 = a2 + kA2Bytes;
 #pragma unroll
-      for (uint32_t kk = 0; kk < 4; ++kk) {
+      for (uint32_t kk = 0; kk < 2; ++kk) {  // K = 32 records as two K = 16 steps
         const uint32_t acc = (i > 0 || kk > 0) ? 1u : 0u;
-        tc::mma_tf32(tmem + kD1Col, tc::sdesc(a1 + kk * 256, 128, 1024), tc::sdesc(b1 + kk * 256, 128, 1024), id1, acc);
-        tc::mma_tf32(tmem + kD2Col, tc::sdesc(a2 + kk * 256, 128, 1024), tc::sdesc(b2 + kk * 256, 128, 1024), id2, acc);
+        tc::mma_f16(tmem + kD1Col, tc::sdesc(a1 + kk * 256, 128, 512), tc::sdesc(b1 + kk * 256, 128, 512), id1, acc);
+        tc::mma_f16(tmem + kD2Col, tc::sdesc(a2 + kk * 256, 128, 512), tc::sdesc(b2 + kk * 256, 128, 512), id2, acc);
       }
       tc::mma_commit(&S.empty[sidx]);
     }
@@ -786,8 +793,8 @@ constexpr uint32_t kBtColsPerGroup = 128;  // A: 64 columns, D: 64 columns
 // are consecutive samples of one or two rays, so at the coarse levels runs
 // of neighbouring lanes share a cell: levels 0..kAggLevels-1 sum each run's
 // corner gradients with shuffles and add them with one atomic per run.
-constexpr int kAggLevels = 7;  // levels whose scatter-add is warp-aggregated (N <= 111)
-static_assert(level_res(kAggLevels - 1) < 128, "cell key packs 7 bits per coordinate");
+constexpr int kAggLevels = 13;  // levels whose scatter-add is warp-aggregated (N <= 776)
+static_assert(level_res(kAggLevels - 1) < 1024, "cell key packs 10 bits per coordinate");
 
 __device__ __forceinline__ void scatter_add_levels(float2* __restrict__ gtable, const DevScene& sc, float3 x,
                                                    const float (&denc)[kEnc], bool valid, uint32_t lane) {
@@ -815,7 +822,7 @@ __device__ __forceinline__ void scatter_add_levels(float2* __restrict__ gtable, 
     }
     // Runs of lanes with the same cell (invalid lanes form runs of their
     // own and add nothing).  N <= 111 here: 7 bits per coordinate.
-    const uint32_t key = valid ? (c.ix | (c.iy << 7) | (c.iz << 14)) : (0x80000000u | lane);
+    const uint32_t key = valid ? (c.ix | (c.iy << 10) | (c.iz << 20)) : (0x80000000u | lane);
     const uint32_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
     const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != key);
     if (heads == 0xffffffffu) {  // no lane shares its cell
@@ -906,25 +913,59 @@ __global__ void pack_bt_images_kernel(const float* __restrict__ w, uint8_t* __re
 
 __device__ __forceinline__ uint32_t f2u(float v) { return __float_as_uint(v); }
 
-// Staging of features f..f+3 (f % 4 == 0) of this thread's record.  The four
-// lanes of a quad hold four consecutive records; a 4x4 transpose inside the
-// quad (two shuffle stages) gives lane q feature f+q of all four records,
-// which is one 16-byte row of the canonical K-major layout: one vector store
-// instead of four scalar ones.  Every lane of the warp must call it.
-__device__ __forceinline__ void stage4(float* arr, int F, uint32_t s, int f, float a0, float a1, float a2, float a3,
-                                       bool stage) {
-  const uint32_t q = threadIdx.x & 3u;
-  const bool odd = q & 1u, hi = q & 2u;
-  float t = __shfl_xor_sync(0xffffffffu, odd ? a0 : a1, 1);
-  if (odd) a0 = t; else a1 = t;
-  t = __shfl_xor_sync(0xffffffffu, odd ? a2 : a3, 1);
-  if (odd) a2 = t; else a3 = t;
-  t = __shfl_xor_sync(0xffffffffu, hi ? a0 : a2, 2);
-  if (hi) a0 = t; else a2 = t;
-  t = __shfl_xor_sync(0xffffffffu, hi ? a1 : a3, 2);
-  if (hi) a1 = t; else a3 = t;
-  if (stage)
-    *reinterpret_cast<float4*>(stage_row(arr, F, s & ~3u) + soff(f + (int)q)) = make_float4(a0, a1, a2, a3);
+// Staging of features f..f+7 (f % 8 == 0) of this thread's record as BF16,
+// in the canonical K-major layout of a 16-bit tensor-core operand with
+// K = record: 8 features x 8 records per 128-byte core matrix (16-byte rows,
+// one feature each), record groups of 8 at 128 B, feature groups of 8 at
+// 512 B; an F-wide array's 32-record tile is F x 64 contiguous bytes.  The
+// eight lanes of an octet hold eight consecutive records; an 8x8 transpose of
+// 16-bit values inside the octet -- packed halves exchanged with the
+// neighbouring lane, then a 4x4 transpose of 32-bit words across lanes 2 and
+// 4 apart, six shuffles -- leaves lane r with feature f + r of all eight
+// records: one 16-byte row.  A warp's 32 records are one tile, so each call
+// writes one contiguous 512-byte block.  Every lane of the warp must call it.
+// Two FP32 values -> packed BF16 (round to nearest even), lo in the low half.
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+__device__ __forceinline__ void stage8(float* arr, int F, uint32_t s, int f, float a0, float a1, float a2, float a3,
+                                       float a4, float a5, float a6, float a7, bool stage) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t w[4] = {bf16x2(a0, a1), bf16x2(a2, a3), bf16x2(a4, a5), bf16x2(a6, a7)};  // low half: even feature
+  // Records 2p and 2p + 1 (lanes r and r ^ 1): the even lane keeps the even
+  // features of both, the odd lane the odd ones.
+  const bool even = (lane & 1u) == 0u;
+  const uint32_t give = even ? 0x7632u : 0x5410u;  // the halves the neighbour keeps
+  const uint32_t r0 = __shfl_xor_sync(0xffffffffu, __byte_perm(w[0], w[1], give), 1);
+  const uint32_t r1 = __shfl_xor_sync(0xffffffffu, __byte_perm(w[2], w[3], give), 1);
+  uint32_t z0, z1, z2, z3;  // z_j: feature 2j + (lane & 1) of records 2p, 2p + 1
+  if (even) {
+    z0 = __byte_perm(w[0], r0, 0x5410u);
+    z1 = __byte_perm(w[1], r0, 0x7610u);
+    z2 = __byte_perm(w[2], r1, 0x5410u);
+    z3 = __byte_perm(w[3], r1, 0x7610u);
+  } else {
+    z0 = __byte_perm(r0, w[0], 0x7610u);
+    z1 = __byte_perm(r0, w[1], 0x7632u);
+    z2 = __byte_perm(r1, w[2], 0x7610u);
+    z3 = __byte_perm(r1, w[3], 0x7632u);
+  }
+  // 4x4 transpose over (record pair p = lane bits 1-2, j).
+  const bool odd = (lane >> 1) & 1u, hi = (lane >> 2) & 1u;
+  uint32_t t = __shfl_xor_sync(0xffffffffu, odd ? z0 : z1, 2);
+  if (odd) z0 = t; else z1 = t;
+  t = __shfl_xor_sync(0xffffffffu, odd ? z2 : z3, 2);
+  if (odd) z2 = t; else z3 = t;
+  t = __shfl_xor_sync(0xffffffffu, hi ? z0 : z2, 4);
+  if (hi) z0 = t; else z2 = t;
+  t = __shfl_xor_sync(0xffffffffu, hi ? z1 : z3, 4);
+  if (hi) z1 = t; else z3 = t;
+  if (stage) {
+    uint8_t* tile = reinterpret_cast<uint8_t*>(arr) + (size_t)(s >> 5) * (size_t)F * 64u;
+    *reinterpret_cast<uint4*>(tile + (f >> 3) * 512 + (lane >> 3) * 128 + (lane & 7u) * 16) = make_uint4(z0, z1, z2, z3);
+  }
 }
 
 __global__ void __launch_bounds__(kBtThreads, 1)
@@ -1012,7 +1053,7 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
         for (int k = 0; k < kEnc; ++k) u[k] = f2u(enc[k]);
         tc::tmem_st32_nowait(a_row, u);
 #pragma unroll
-        for (int k = 0; k < kEnc; k += 4) stage4(st.enc, kEnc, s, k, enc[k], enc[k + 1], enc[k + 2], enc[k + 3], stage);
+        for (int k = 0; k < kEnc; k += 8) stage8(st.enc, kEnc, s, k, enc[k + 0], enc[k + 1], enc[k + 2], enc[k + 3], enc[k + 4], enc[k + 5], enc[k + 6], enc[k + 7], stage);
       }
       if (!mma(0)) break;
       uint64_t m_h1 = 0, m_g1 = 0, m_g2 = 0;
@@ -1029,7 +1070,7 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
           }
           tc::tmem_st32_nowait(a_row + 32 * c, u);
 #pragma unroll
-          for (int j = 0; j < 32; j += 4) stage4(act, kHid, s, 32 * c + j, v[j], v[j + 1], v[j + 2], v[j + 3], stage);
+          for (int j = 0; j < 32; j += 8) stage8(act, kHid, s, 32 * c + j, v[j + 0], v[j + 1], v[j + 2], v[j + 3], v[j + 4], v[j + 5], v[j + 6], v[j + 7], stage);
         }
       };
       relu64(st.h1, m_h1);
@@ -1052,7 +1093,7 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
         }
         tc::tmem_st32_nowait(a_row, u);
 #pragma unroll
-        for (int k = 0; k < kCIn; k += 4) stage4(st.cin, kCIn, s, k, cin[k], cin[k + 1], cin[k + 2], cin[k + 3], stage);
+        for (int k = 0; k < kCIn; k += 8) stage8(st.cin, kCIn, s, k, cin[k + 0], cin[k + 1], cin[k + 2], cin[k + 3], cin[k + 4], cin[k + 5], cin[k + 6], cin[k + 7], stage);
       }
       if (!mma(2)) break;
       relu64(st.g1, m_g1);
@@ -1069,8 +1110,7 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
 #pragma unroll
         for (int k = 0; k < 16; ++k) w16[k] = k < 3 ? f2u(dl[k]) : 0u;
         tc::tmem_st16_nowait(a_row, w16);
-        stage4(st.dlog, kFDlog, s, 0, dl[0], dl[1], dl[2], 0.0f, stage);
-        stage4(st.dlog, kFDlog, s, 4, 0.0f, 0.0f, 0.0f, 0.0f, stage);
+        stage8(st.dlog, kFDlog, s, 0, dl[0], dl[1], dl[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, stage);
       }
       // Masked D[:, :64] -> staging, next A.
       auto mask64 = [&](float* delta, uint64_t m) {
@@ -1084,7 +1124,7 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
           }
           tc::tmem_st32_nowait(a_row + 32 * c, u);
 #pragma unroll
-          for (int j = 0; j < 32; j += 4) stage4(delta, kHid, s, 32 * c + j, v[j], v[j + 1], v[j + 2], v[j + 3], stage);
+          for (int j = 0; j < 32; j += 8) stage8(delta, kHid, s, 32 * c + j, v[j + 0], v[j + 1], v[j + 2], v[j + 3], v[j + 4], v[j + 5], v[j + 6], v[j + 7], stage);
         }
       };
       if (!mma(5)) break;
@@ -1104,8 +1144,7 @@ backward_tc_kernel(const SampleRec* __restrict__ recs, uint32_t first, uint32_t 
         for (int m = 0; m < 16; ++m) w16[m] = f2u(dout[m]);
         tc::tmem_st16_nowait(a_row, w16);
 #pragma unroll
-        for (int m = 0; m < kDOut; m += 4)
-          stage4(st.dout, kDOut, s, m, dout[m], dout[m + 1], dout[m + 2], dout[m + 3], stage);
+        for (int m = 0; m < kDOut; m += 8) stage8(st.dout, kDOut, s, m, dout[m + 0], dout[m + 1], dout[m + 2], dout[m + 3], dout[m + 4], dout[m + 5], dout[m + 6], dout[m + 7], stage);
       }
       if (!mma(8)) break;
       mask64(st.dh1, m_h1);
