@@ -297,13 +297,15 @@ typedef struct nes_train_config {
 } nes_train_config;
 
 /* lr 1e-2, betas (0.9, 0.99), eps 1e-15, depth weight 0.1, 2^18 rays,
- * tensor-core weight gradients. */
+ * the tensor-core mode (exact_weight_grads = 0). */
 void nes_train_config_default(nes_train_config *cfg);
 
 /* The student must be an NES_PREC_FP32 context; its table and weights are
  * updated in place by the step calls.  batch_rays <= 2^20.  Device memory:
- * 64 B per ray per march step (1024 steps) of scratch plus ~3.9 GB of
- * per-sample staging and 4x the table for gradient and Adam moments. */
+ * 64 B per ray per march step (1024 steps) of scratch (per-sample state and
+ * the sample list / adjoint records), ~3.9 GB of per-sample staging for the
+ * weight gradients, 4x the table for gradient and Adam moments, and ~160 KB
+ * of weight operand images. */
 int nes_trainer_create(nes_ctx *student, const nes_train_config *cfg, nes_trainer **out);
 void nes_trainer_destroy(nes_trainer *tr);
 
