@@ -815,13 +815,24 @@ __device__ __forceinline__ void scatter_add_levels(float2* __restrict__ gtable, 
         d1 = denc[2 * k + 1];
       }
     if (l >= kAggLevels) {
-      if (valid)
+      if (valid && !((sc.dense_mask >> l) & 1u) && (c.ix & 1u) == 0u) {
+        // Hashed level, even x: the x prime is 1, so corners k and k + 1
+        // are the aligned entry pair {i, i ^ 1}; one 16-byte atomic each.
+#pragma unroll
+        for (int k = 0; k < 8; k += 2) {
+          const uint32_t i = idx[k];
+          const float4 v = (i & 1u) ? make_float4(w[k + 1] * d0, w[k + 1] * d1, w[k] * d0, w[k] * d1)
+                                    : make_float4(w[k] * d0, w[k] * d1, w[k + 1] * d0, w[k + 1] * d1);
+          atomicAdd(reinterpret_cast<float4*>(gt + (i & ~1u)), v);
+        }
+      } else if (valid) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) atomicAdd(gt + idx[k], make_float2(w[k] * d0, w[k] * d1));
+      }
       continue;
     }
     // Runs of lanes with the same cell (invalid lanes form runs of their
-    // own and add nothing).  N <= 111 here: 7 bits per coordinate.
+    // own and add nothing).  N <= 776 here: 10 bits per coordinate.
     const uint32_t key = valid ? (c.ix | (c.iy << 10) | (c.iz << 20)) : (0x80000000u | lane);
     const uint32_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
     const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != key);
@@ -1700,8 +1711,10 @@ int loss_and_grad(nes_trainer* t, int n, double* loss) {
     pack_bt_images_kernel<<<(kBtImageBytes / 4 + 255) / 256, 256, 0, t->st>>>(c->d_weights, t->d_bimg);
     TR_CUDA(cudaGetLastError());
   }
-  for (uint32_t first = 0; first < total; first += t->chunk) {
-    const uint32_t cnt = total - first < t->chunk ? total - first : t->chunk;
+  // BF16 staging (tensor-core mode) holds twice the records in the same bytes.
+  const uint32_t chunk = t->cfg.exact_weight_grads ? t->chunk : 2u * t->chunk;
+  for (uint32_t first = 0; first < total; first += chunk) {
+    const uint32_t cnt = total - first < chunk ? total - first : chunk;
     if (t->cfg.exact_weight_grads) {
       backward_kernel<<<(cnt + kBwdThreads - 1) / kBwdThreads, kBwdThreads, kSmemB, t->st>>>(
           t->d_recs, first, cnt, t->d_rays, c->scene, sg, t->d_gtable);
