@@ -4,9 +4,11 @@
 // leave tensor memory, overlapped with the hash-grid gathers by warp
 // specialisation.
 //
-// Why this shape: the march is bound by the ~128 scattered 4-byte table
-// gathers per sample, and their speed depends on the L1 cache (a 28 KiB L1
-// made them ~2.5x slower than a 192 KiB one).  So shared memory holds only
+// Why this shape: the march is bound by its hash-table gathers through the
+// L1 data pipe (per sample 16 levels x 8 corners: the recorded levels as one
+// 32-byte per-cell record, the others as eight scattered 4-byte gathers), and
+// their speed depends on the L1 cache (a 28 KiB L1 made them ~2.5x slower
+// than a 192 KiB one).  So shared memory holds only
 // the MLP weights (the B operands, 20 KiB) and small per-row hand-off arrays,
 // within the 32 KiB configuration; every A operand (encoded features, hidden
 // layers, colour input) lives in TMEM and feeds tcgen05.mma directly.
