@@ -45,9 +45,9 @@ GATHER_BYTES = {"fp32": 1024, "fp16": 512}  # 16 levels x 8 corners x 2 features
 # dram__bytes_read.sum + dram__bytes_write.sum of one full 1920x1080 march
 # launch: the tensor-core march with records of levels 0..12 from a 1-pass
 # ncu capture of `bench.py --steps 1 --warmup 1 --precision tc --no-extras
-# --no-cpu-baseline --e2e-steps 1` (42.13 GB + 25.9 MB), the FP32 march from
+# --no-cpu-baseline --e2e-steps 1` (49.23 GB + 17.7 MB), the FP32 march from
 # a capture of the same command with --precision fp32.
-DRAM_BYTES_PER_LAUNCH = {"fp16": 42.130e9 + 25.87e6, "fp32": 73.651e6 + 7.437e6}
+DRAM_BYTES_PER_LAUNCH = {"fp16": 49.23e9 + 17.72e6, "fp32": 73.651e6 + 7.437e6}
 DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full 1920x1080 launch (1 pass)"
 # The tensor-core march's binding unit is the L1 data pipe (ncu names it as
 # the limiter: LSU wavefronts at 66 % of peak, long-scoreboard stalls
@@ -57,7 +57,7 @@ DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full 1920x1
 # wavefronts.sum / the launch's samples), and the pipe's peak of one wavefront
 # per SM per cycle (l1tex__data_pipe_lsu_wavefronts.sum.peak_sustained = the
 # SM count).
-L1_WF_PER_SAMPLE = {("fp16", 13): 5228328301 / 285031892}  # 18.34
+L1_WF_PER_SAMPLE = {("fp16", 13): 5250204369 / 285031892}  # 18.42
 L1_WF_PER_SM_CYCLE = 1.0
 L1_WF_SOURCE = ("ncu l1tex__data_pipe_lsu_wavefronts.sum of one full 1920x1080 launch (1 pass) / its samples; "
                 "peak = 1 wavefront per SM per cycle x SMs x the median SM clock sampled during the timed steps")
@@ -439,9 +439,9 @@ def roofline_terms(head, kind, tf_sust, src, hbm, sms, rec_levels):
                                 "and the FP32 RGB + depth written (16 B per pixel).  The measured excess is "
                                 "by design: the per-cell corner records of levels 7-12 (copies of table "
                                 "entries, 24 GB) are read from HBM, one 32-byte sector per level and sample "
-                                "(~1.7 TB/s, a quarter of HBM bandwidth), in place of eight scattered L1/L2 "
-                                "gathers each; with records of levels 0-9 only (2.8 GB per launch) the march "
-                                "is 6 % slower",
+                                "(~2 TB/s, under a third of HBM bandwidth; levels 10-12 with an L2 "
+                                "evict-first policy), in place of eight scattered L1/L2 gathers each; with "
+                                "records of levels 0-9 only (2.8 GB per launch) the march is 6-8 % slower",
                 "hbm_peak_gbs": hbm,
                 "limiter": "hash-table gathers through L1: L1 data pipe at 66% of its wavefront rate, "
                            "long-scoreboard stalls dominant, tensor pipe 10%, DRAM 3% (ncu full sections, "
