@@ -1,5 +1,6 @@
 """The integration guide's binding examples (the C++ and ctypes blocks a
-neserver maintainer would add) against the real C ABI: every C++ block compiles (g++ -fsyntax-only) against include/nes_gb300.h with stand-ins
+neserver maintainer would add) against the real C ABI: every C++ block
+compiles (g++ -fsyntax-only) against include/nes_gb300.h with stand-ins
 for neserver's own types (protobuf messages, AVFrame, the RenderedFrame
 constructor), and the raw ctypes stub resolves its symbol in the built
 library.  No GPU is used."""
