@@ -7,9 +7,11 @@
 // Per step:
 //  1. rays: (view, pixel) pairs (drawn from the step seed or given) -> the
 //     FP32 ray set-up of rendering, with the target colour and depth;
-//  2. forward: the rays' occupied steps listed (thread per ray), the FP32
-//     field evaluated at every listed sample (thread per sample), then each
-//     ray composited with early termination (thread per ray), keeping each
+//  2. forward: the rays' occupied steps listed (thread per ray), the field
+//     evaluated at every listed sample (by default the MLP products on the
+//     tensor cores as 3xTF32, FP32-level; exact_weight_grads = 1: FP32 on the
+//     CUDA cores), then each ray composited with early termination (thread
+//     per ray), keeping each
 //     evaluated sample's t, alpha, transmittance and colour in the ray's
 //     scratch row; loss; then walk the samples backwards carrying
 //     A = dL/dT_k for each one's compositing adjoint
@@ -26,10 +28,12 @@
 //     FP32 gradient table with float2 atomics, and stage every layer's input
 //     activations and output deltas.  By default the ten layer products of
 //     the recompute and the backpropagation run on the tensor cores
-//     (backward_tc_kernel, tcgen05 kind::tf32); exact_weight_grads = 1 keeps
-//     them in FP32 on the CUDA cores (backward_kernel);
+//     (backward_tc_kernel, tcgen05 kind::tf32) and the staging is BF16;
+//     exact_weight_grads = 1 keeps them in FP32 on the CUDA cores
+//     (backward_kernel) with FP32 staging;
 //  4. weight gradients: per layer dW[out][in] += sum_s delta[s][out] act[s][in]
-//     over the chunk (dw_kernel, register-tiled split-K reduction);
+//     over the chunk (by default dw_tc_kernel, tcgen05 kind::f16 with BF16
+//     operands; exact: dw_kernel, register-tiled split-K reduction);
 //  5. Adam on the table and the weights (bias-corrected); gradients zeroed.
 // An FP64 variant of the loss evaluates the same function with one parameter
 // perturbed, for central finite differences.
@@ -77,7 +81,8 @@ struct SampleRec {  // compacted sample with its compositing adjoint
 };
 
 // Per-sample staging of the weight-gradient reductions, in 32-sample
-// tiles.  Each tile of an F-wide array (F a multiple of 8) is one
+// tiles (FP32 layout of the strict mode; the tensor-core mode stages BF16,
+// see stage8).  Each tile of an F-wide array (F a multiple of 8) is one
 // contiguous block of F x 32 floats in the canonical K-major layout of the
 // tensor core's shared-memory operands, no swizzle, K = sample: 8-feature x
 // 4-sample core matrices of 128 bytes, the 8 core matrices of a feature
@@ -100,7 +105,7 @@ __device__ __forceinline__ float* stage_row(float* a, int F, uint32_t s) {
 }
 __host__ __device__ constexpr int soff(int f) { return (f >> 3) * 256 + (f & 7) * 4; }
 
-// Forward evaluation: 128-thread blocks, three resident per SM at its 135 registers.
+// FP32 forward evaluation: 128-thread blocks, three resident per SM at its 167 registers.
 // Backward: 256-thread blocks capped at 128 registers, two resident per SM
 // (16 warps) with one shared copy of the weights per block, which leaves
 // L1 for the table gathers.
@@ -159,21 +164,24 @@ struct RayOut {  // composited result of one training ray
   int pad;
 };
 
-// Forward, in three passes, so that the per-sample FP32 MLP runs with every
-// lane of a warp busy (marched one ray per thread, the lanes whose ray is at
-// an empty step would idle while the others evaluate):
+// Forward, in three passes, so that the per-sample MLP runs with every lane
+// of a warp busy (marched one ray per thread, the lanes whose ray is at an
+// empty step would idle while the others evaluate) or on the tensor cores in
+// 128-sample tiles:
 //  1. enumerate_kernel, thread per ray: the ray's occupied steps in order --
 //     the march's sample set before early termination -- listed contiguously
 //     as (ray, k | step << 16), k the sample's index along the ray;
-//  2. eval_kernel, thread per listed sample: the FP32 encoding and MLPs at
-//     that sample, its t, alpha and colour written to the ray's scratch row k
-//     (a warp's samples are consecutive samples of one or two rays: coherent
-//     gathers);
+//  2. eval_kernel (FP32, thread per listed sample) or eval_tc_kernel (the
+//     MLP products on tcgen05 as 3xTF32, thread = TMEM lane per sample): the
+//     encoding and MLPs at that sample, its t, alpha and colour written to the
+//     ray's scratch row k (a warp's samples are consecutive samples of one or
+//     two rays: coherent gathers);
 //  3. composite_kernel, thread per ray: the ray's rows in order, composited
 //     and stopped at T < kTStop exactly as a one-pass march composites, with
 //     each row's transmittance and the ray's RayOut filled in.
-// Per sample the arithmetic is the one-pass march's; only the samples after
-// an early termination are evaluated and then left unused.
+// With eval_kernel the per-sample arithmetic is the one-pass FP32 march's;
+// only the samples after an early termination are evaluated and then left
+// unused.
 constexpr uint32_t kListStepShift = 16;
 static_assert(kMaxSteps <= (1 << kListStepShift), "k and step share one word");
 
