@@ -19,8 +19,9 @@
 //    FP16 table, writes the 32 FP16 features as its TMEM lane of the tile (16
 //    columns), hands the row's ray id, flags and t over in shared memory and
 //    marks the tile full.  It never waits for results: only for
-//    its tile buffer to be free again (two buffers), which the MLP's first
-//    layer releases through its MMA commit.  Encoder warps run independently.
+//    its tile buffer to be free again (two buffers), which the MLP side
+//    releases once its first layer is done and every row's hand-off has been
+//    read.  Encoder warps run independently.
 //  - MLP thread = TMEM lane = tile row.  One thread issues each layer
 //    (32->64, 64->16, 32->64, 64->64, 64->16 [3 used]) as tcgen05.mma
 //    kind::f16 with A from TMEM and B from shared memory, FP32 accumulators in
@@ -324,7 +325,7 @@ march_tc_kernel(const __grid_constant__ Src src, const DevScene sc, const DevScr
       uint64_t* b = reinterpret_cast<uint64_t*>(Gk + kGOffBar);
       tc::mbar_init(b + 0, kRoleThreads);  // full: every encoder thread arrives
       tc::mbar_init(b + 1, kRoleThreads);
-      tc::mbar_init(b + 2, 1);             // free: the layer-1 commit (or the stop) arrives
+      tc::mbar_init(b + 2, 1);             // free: MLP row 0 arrives after layer 1 (or at the stop)
       tc::mbar_init(b + 3, 1);
       tc::mbar_init(b + 4, 1);             // mma: commit of each layer
       *reinterpret_cast<uint32_t*>(Gk + kGOffDone) = 0u;
@@ -424,9 +425,13 @@ march_tc_kernel(const __grid_constant__ Src src, const DevScene sc, const DevScr
       }
       const uint32_t a_col = enc_cols + 16 * b;  // encoded features of this tile
       // density 32 -> 64 -> 16 (the first layer is the features' last reader)
-      layer(a_col, kWoffDW1, 32, id64, bar + 2 + b);
+      layer(a_col, kWoffDW1, 32, id64, nullptr);
       relu_to_h(d_row, h_row);
       if (sync_bad()) { fail = true; break; }
+      // The tile buffer goes back to the encoders once its features have
+      // been read (the first layer is complete) and every row's hand-off
+      // entry has been read (the barrier above).
+      if (row == 0) tc::mbar_arrive(bar + 2 + b);
       layer(h_col, kWoffDW2, 64, id16, nullptr);
       float sigma;
       {
