@@ -331,15 +331,27 @@ adjoint_kernel(const TrainRay* __restrict__ rays, const RayOut* __restrict__ rou
       const float3 o = make_float3(r.ox, r.oy, r.oz), d = make_float3(r.dx, r.dy, r.dz);
       const ScratchSample* row = scratch + (size_t)i * kMaxSteps;
       float A = 0.0f;
-      for (int k = K - 1; k >= 0; --k) {
-        const ScratchSample q = row[k];
-        const float w = q.T * q.alpha;
-        const float T1 = q.T - w;
-        const float gw = fmaf(gC0, q.cr, fmaf(gC1, q.cg, fmaf(gC2, q.cb, gD * q.t)));
-        const float dsig = kDt * T1 * (gw - A);
-        const float3 x = sample_pos(o, d, q.t);
-        recs[base + k] = SampleRec{x.x, x.y, x.z, (uint32_t)i, dsig, gC0 * w, gC1 * w, gC2 * w};
-        A = fmaf(gw, q.alpha, A * (1.0f - q.alpha));
+      // Rows in batches of kBatch from the back, all loaded before the
+      // first is used (the loads do not wait on the sweep's arithmetic).
+      constexpr int kBatch = 8;
+      for (int k1 = K - 1; k1 >= 0; k1 -= kBatch) {
+        ScratchSample qb[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u)
+          if (k1 - u >= 0) qb[u] = row[k1 - u];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int k = k1 - u;
+          if (k < 0) break;
+          const ScratchSample& q = qb[u];
+          const float w = q.T * q.alpha;
+          const float T1 = q.T - w;
+          const float gw = fmaf(gC0, q.cr, fmaf(gC1, q.cg, fmaf(gC2, q.cb, gD * q.t)));
+          const float dsig = kDt * T1 * (gw - A);
+          const float3 x = sample_pos(o, d, q.t);
+          recs[base + k] = SampleRec{x.x, x.y, x.z, (uint32_t)i, dsig, gC0 * w, gC1 * w, gC2 * w};
+          A = fmaf(gw, q.alpha, A * (1.0f - q.alpha));
+        }
       }
     }
   }
