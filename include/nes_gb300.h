@@ -135,8 +135,10 @@ int nes_render_views(nes_ctx *ctx, const nes_view *views, int nviews, float *con
 /* Pose -> YUV end to end for one view: render, RGB24 quantise, convert to
  * YUV420P and pack depth to uint16 mm on the device, then copy the planes to
  * the caller's HOST buffers (pinned for best speed).  y/u/v follow
- * linesize[3] (chroma planes are ceil(W/2) x ceil(H/2)); depth_mm_host is
- * W*H uint16 (may be NULL).  Blocks until the host buffers are filled. */
+ * linesize[3] (chroma planes are ceil(W/2) x ceil(H/2)); only the visible
+ * bytes of each row are written, the row padding up to the linesize is left
+ * as it was.  depth_mm_host is W*H uint16 (may be NULL).  Blocks until the
+ * host buffers are filled. */
 int nes_render_yuv(nes_ctx *ctx, const nes_view *view, uint8_t *y_host, uint8_t *u_host,
                    uint8_t *v_host, const int linesize[3], uint16_t *depth_mm_host);
 

@@ -328,11 +328,14 @@ int nes_render_yuv_views(nes_ctx* c, const nes_view* views, int nviews, uint8_t*
   }
   frame_batch_index(&fb);
   NES_CUDA(launch_frame_out(fb, c->stream));
+  // Only the visible bytes of each row go back: the caller's row padding is
+  // left as it was (the device planes' padding holds nothing defined).
+  const int cw = (w + 1) / 2;
   for (int i = 0; i < nviews; ++i) {
     const FrameOut& F = fb.f[i];
-    NES_CUDA(cudaMemcpyAsync(y_host[i], F.y, ysz, cudaMemcpyDeviceToHost, c->stream));
-    NES_CUDA(cudaMemcpyAsync(u_host[i], F.u, usz, cudaMemcpyDeviceToHost, c->stream));
-    NES_CUDA(cudaMemcpyAsync(v_host[i], F.v, vsz, cudaMemcpyDeviceToHost, c->stream));
+    NES_CUDA(cudaMemcpy2DAsync(y_host[i], linesize[0], F.y, linesize[0], w, h, cudaMemcpyDeviceToHost, c->stream));
+    NES_CUDA(cudaMemcpy2DAsync(u_host[i], linesize[1], F.u, linesize[1], cw, ch, cudaMemcpyDeviceToHost, c->stream));
+    NES_CUDA(cudaMemcpy2DAsync(v_host[i], linesize[2], F.v, linesize[2], cw, ch, cudaMemcpyDeviceToHost, c->stream));
     if (F.depth_mm)
       NES_CUDA(cudaMemcpyAsync(depth_mm_host[i], F.depth_mm, px * sizeof(uint16_t), cudaMemcpyDeviceToHost,
                                c->stream));

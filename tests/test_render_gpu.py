@@ -317,3 +317,17 @@ def test_record_depth_does_not_change_the_render(nes_lib, cuda):
     assert na == nb
     for (ra, da), (rb, db) in zip(a, b):
         assert np.array_equal(ra, rb) and np.array_equal(da, db)
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (1, 9), (9, 1), (31, 3), (129, 2)])
+def test_degenerate_and_odd_views_vs_oracle(renderer, cuda, scene0, nes_lib, W, H):
+    """Views far smaller than one 128-row tile of the tensor-core march, a
+    single row or column, odd widths and one row wider than a tile: every
+    pixel against the oracle and the exact sample count."""
+    M = nes_lib.shell_poses(0, 3, 1.5, 1.5)[1]
+    f = nes_lib.focal_from_fov(W, 90.0)
+    (rgb, dep), = render_gpu(renderer, cuda, [(M, W, H, f)])
+    orgb, odep, osamples = scene0.render(M, W, H, f)
+    assert renderer.last_sample_count() == osamples
+    assert psnr(rgb, orgb) >= PSNR_MIN
+    assert np.abs(dep - odep).max() <= DEPTH_TOL

@@ -199,3 +199,37 @@ def test_render_yuv_views_stereo_matches_single_views(rtc, cuda, nes_lib):
         rtc.render_yuv(v, one[0].data_ptr(), one[1].data_ptr(), one[2].data_ptr(), ls, one[3].data_ptr())
         for a, b in zip(got, one):
             assert np.array_equal(a.numpy(), b.numpy())
+
+
+@pytest.mark.parametrize("W,H", [(33, 17), (1, 1), (3, 5)])
+@pytest.mark.parametrize("prec", ["fp32", "tc"])
+def test_render_yuv_odd_sizes(cuda, nes_lib, oracle_mod, prec, W, H):
+    """nes_render_yuv at odd widths and heights (chroma planes of ceil(W/2) x
+    ceil(H/2)): the fused frame output gives the bytes of the separate
+    conversions of the same render in the visible part of every row, and the
+    row padding of the caller's planes is left as it was."""
+    torch = cuda
+    p = nes_lib.PREC_FP32 if prec == "fp32" else nes_lib.PREC_FP16_TC
+    M = nes_lib.shell_poses(0, 100, 1.5, 1.5)[5]
+    focal = nes_lib.focal_from_fov(W, 90.0)
+    view = nes_lib.make_view(M, W, H, focal)
+    ls = nes_lib.linesizes(W)
+    ch = (H + 1) // 2
+    y = torch.zeros(ls[0] * H, dtype=torch.uint8).pin_memory()
+    u = torch.zeros(ls[1] * ch, dtype=torch.uint8).pin_memory()
+    v = torch.zeros(ls[2] * ch, dtype=torch.uint8).pin_memory()
+    dmm = torch.zeros(W * H, dtype=torch.int16).pin_memory()
+    with nes_lib.Renderer(precision=p, max_pixels=64 * 64) as r:
+        r.render_yuv(view, y.data_ptr(), u.data_ptr(), v.data_ptr(), ls, dmm.data_ptr())
+        rgb = torch.empty(W * H * 3, device="cuda")
+        dep = torch.empty(W * H, device="cuda")
+        r.render_views([view], [rgb.data_ptr()], [dep.data_ptr()])
+        torch.cuda.synchronize()
+    rgb24 = oracle_mod.rgb_to_rgb24(rgb.cpu().numpy())
+    oy, ou, ov = oracle_mod.rgb24_to_yuv420p(rgb24, W, H, W * 3, ls)
+    cw = (W + 1) // 2
+    for got, want, l, w, h in ((y, oy, ls[0], W, H), (u, ou, ls[1], cw, ch), (v, ov, ls[2], cw, ch)):
+        g = got.numpy().reshape(h, l)
+        assert np.array_equal(g[:, :w], want.reshape(h, l)[:, :w])
+        assert not g[:, w:].any()  # the padding keeps the caller's zeros
+    assert np.array_equal(dmm.numpy().view(np.uint16), oracle_mod.depth_pack_u16mm(dep.cpu().numpy()))
