@@ -372,6 +372,17 @@ __global__ void __launch_bounds__(kGlueThreads) frame_out_kernel(const __grid_co
     }
     F.u[(size_t)cy * F.ls1 + cx] = clamp8((kUR * sr + kUG * sg + kUB * sb + (128 << 18) + (1 << 17)) >> 18);
     F.v[(size_t)cy * F.ls2 + cx] = clamp8((kVR * sr + kVG * sg + kVB * sb + (128 << 18) + (1 << 17)) >> 18);
+    if (cx == (int)cw - 1) {
+      // The row padding up to each linesize is zeroed, so no plane carries
+      // bytes of an earlier frame (serving reuses its output arena).
+      for (int dy = 0; dy < 2; ++dy) {
+        const int yy = 2 * cy + dy;
+        if (yy < F.h)
+          for (int xx = F.w; xx < F.ls0; ++xx) F.y[(size_t)yy * F.ls0 + xx] = 0;
+      }
+      for (int xx = (int)cw; xx < F.ls1; ++xx) F.u[(size_t)cy * F.ls1 + xx] = 0;
+      for (int xx = (int)cw; xx < F.ls2; ++xx) F.v[(size_t)cy * F.ls2 + xx] = 0;
+    }
   }
 }
 

@@ -209,3 +209,23 @@ def test_queue_delay_bound_rejects_late_requests(nes_lib, rtc):
             srv.close()
     assert admitted[0.0] == 8
     assert 1 <= admitted[100.0] < 8, admitted
+
+
+def test_plane_padding_is_zero(nes_lib, server):
+    """Served planes carry zeros in their row padding: the output arena is
+    reused from request to request, and no request sees bytes of an earlier
+    frame there."""
+    poses = nes_lib.shell_poses(4, 2, 1.5, 1.5)
+    t = server.submit(views_for(nes_lib, poses[0], 1280, 720, 90.0, False))
+    assert server.wait(t).status == 0
+    server.release(t)
+    for W, H in ((33, 17), (650, 31)):
+        t = server.submit(views_for(nes_lib, poses[1], W, H, 90.0, False))
+        res = server.wait(t)
+        assert res.status == 0
+        y, u, v, _ = server.fetch(res)
+        ls, ch, cw = list(res.linesize), (H + 1) // 2, (W + 1) // 2
+        assert ls[0] > W and ls[1] > cw
+        assert not y.reshape(H, ls[0])[:, W:].any()
+        assert not u.reshape(ch, ls[1])[:, cw:].any() and not v.reshape(ch, ls[2])[:, cw:].any()
+        server.release(t)
