@@ -220,7 +220,7 @@ typedef struct nes_result {
   int32_t status;  /* NES_OK, or the error of the batch */
   uint32_t nviews;
   uint32_t width, height;
-  int32_t linesize[3];        /* YUV420P plane linesizes (32-byte aligned) */
+  int32_t linesize[3];        /* YUV420P plane linesizes (32-byte aligned; row padding zeroed) */
   uint8_t *y_dev[2], *u_dev[2], *v_dev[2];
   uint16_t *depth_mm_dev[2];  /* W*H uint16 millimetres per view */
   double latency_ms;          /* submit -> YUV ready on the device */
