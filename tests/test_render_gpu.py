@@ -331,3 +331,24 @@ def test_degenerate_and_odd_views_vs_oracle(renderer, cuda, scene0, nes_lib, W, 
     assert renderer.last_sample_count() == osamples
     assert psnr(rgb, orgb) >= PSNR_MIN
     assert np.abs(dep - odep).max() <= DEPTH_TOL
+
+
+def test_view_that_misses_the_volume(renderer, cuda, scene0, nes_lib):
+    """A camera outside the unit cube looking away from it: every ray misses
+    (RGB 0, depth 0, no samples), alone and batched ahead of a view that
+    hits, which still matches the oracle."""
+    away = nes_lib.look_at((0.5, 0.5, 3.0), (0.5, 0.5, 6.0))
+    hit = nes_lib.shell_poses(0, 3, 1.5, 1.5)[0]
+    W, H = 40, 30
+    f = nes_lib.focal_from_fov(W, 90.0)
+    _, _, osamples_away = scene0.render(away, W, H, f)
+    assert osamples_away == 0
+    (rgb, dep), = render_gpu(renderer, cuda, [(away, W, H, f)])
+    assert renderer.last_sample_count() == 0
+    assert not rgb.any() and not dep.any()
+    (rgb2, dep2), (rgb3, dep3) = render_gpu(renderer, cuda, [(away, W, H, f), (hit, W, H, f)])
+    orgb, odep, osamples = scene0.render(hit, W, H, f)
+    assert renderer.last_sample_count() == osamples
+    assert not rgb2.any() and not dep2.any()
+    assert psnr(rgb3, orgb) >= PSNR_MIN
+    assert np.abs(dep3 - odep).max() <= DEPTH_TOL

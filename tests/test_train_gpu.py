@@ -247,3 +247,38 @@ def test_trainer_errors(nes_lib, setup, cuda):
     assert np.isfinite(t.step_rays(_pairs(64, len(views), 1)))
     t.close()
     r.close()
+
+
+@pytest.mark.parametrize("exact", [1, 0])
+def test_batch_whose_rays_all_miss(nes_lib, cuda, exact):
+    """Rays of a view that looks away from the volume: no samples, so the
+    sample list, the records and the backward chunks are all empty; the loss
+    is the targets' own (student and teacher both render 0 there), the
+    gradient is 0, and a batch mixing such rays with hitting ones gives the
+    hitting rays' gradient scaled by the batch size."""
+    torch = cuda
+    away = (nes_lib.look_at((0.5, 0.5, 3.0), (0.5, 0.5, 6.0)), W, H, nes_lib.focal_from_fov(W, 30.0))
+    views = _views(nes_lib) + [away]
+    nv = len(views)
+    teacher = nes_lib.Renderer(precision=nes_lib.PREC_FP32, seed=1, log2_table_size=LOG2T, max_pixels=nv * W * H)
+    rgb = torch.empty((nv * W * H, 3), device="cuda", dtype=torch.float32)
+    dep = torch.empty((nv * W * H,), device="cuda", dtype=torch.float32)
+    teacher.render_views([nes_lib.make_view(*v) for v in views],
+                         [rgb[i * W * H:].data_ptr() for i in range(nv)], [dep[i * W * H:].data_ptr() for i in range(nv)])
+    torch.cuda.synchronize()
+    teacher.close()
+    r, t = _student(nes_lib, (views, rgb, dep), exact_weight_grads=exact)
+    try:
+        miss = np.stack([np.full(64, nv - 1), np.arange(64) % (W * H)], 1).astype(np.int32)
+        loss, gt, gw = t.grad(miss, TABLE_FLOATS)
+        assert t.last_samples() == 0
+        assert loss == 0.0 and not gt.any() and not gw.any()
+        hits = _pairs(64, nv - 1, 11)
+        lh, gth, gwh = t.grad(hits, TABLE_FLOATS)
+        lm, gtm, gwm = t.grad(np.concatenate([hits, miss]), TABLE_FLOATS)
+        # The loss is a mean over the batch: the missing rays add 0 and halve it.
+        assert lm == pytest.approx(lh / 2, rel=1e-6)
+        assert _close(2 * gtm, gth, 1e-5, 1e-4) and _close(2 * gwm, gwh, 1e-5, 1e-4)
+    finally:
+        t.close()
+        r.close()
