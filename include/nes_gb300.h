@@ -127,14 +127,19 @@ int nes_tcp_serve(nes_ctx *ctx, const char *bind_addr, uint16_t port, const vola
                   uint16_t *bound_port, uint64_t *frames_served);
 
 /* Device-native render of n views in one batch (rays of all views share
- * one march).  rgb_dev[i]: W*H*3 floats (HWC), depth_dev[i]: W*H floats
- * (expected depth, 0 for rays that miss); either may be NULL. */
+ * one march): the renderer's work behind the round trip of
+ * src/server.cpp:161-194 with the frame left on the device, and both eyes
+ * of a stereo request at once where neserver asks for them one at a time
+ * (src/server.cpp:144-153).  rgb_dev[i]: W*H*3 floats (HWC), depth_dev[i]:
+ * W*H floats (expected depth, 0 for rays that miss); either may be NULL. */
 int nes_render_views(nes_ctx *ctx, const nes_view *views, int nviews, float *const *rgb_dev,
                      float *const *depth_dev, void *stream);
 
 /* Pose -> YUV end to end for one view: render, RGB24 quantise, convert to
  * YUV420P and pack depth to uint16 mm on the device, then copy the planes to
- * the caller's HOST buffers (pinned for best speed).  y/u/v follow
+ * the caller's HOST buffers (pinned for best speed): the renderer round trip
+ * (src/server.cpp:161-194) and RenderedFrame::convert_frame
+ * (include/base/video/rendered_frame.h:24-33) in one call.  y/u/v follow
  * linesize[3] (chroma planes are ceil(W/2) x ceil(H/2)); only the visible
  * bytes of each row are written, the row padding up to the linesize is left
  * as it was.  depth_mm_host is W*H uint16 (may be NULL).  Blocks until the
